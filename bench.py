@@ -1,0 +1,330 @@
+"""Benchmark of the two-electron ZV-MC path on one GB300 (or N replicas).
+
+Workload (default): H2O, 26-function STO basis, 20-Gaussian fits, all 61,776 unique (ik|jl),
+2^26 walker pairs; one step = the reference driver's whole job (src/two_e_slater.F90:219-564):
+Schwarz diagonal + analytic Gaussian-fit ERIs (FP64) + ZV-MC correction (shared-walker
+estimator, split-BF16 tcgen05 contraction) + merge.  Metric: unique ERIs per second of job
+wall time, with the job's largest MC error reported (target sigma <= 1e-6 Ha).
+
+Also measured: the same GPU's FP64 plain path (faithful per-pair estimator in FP64; its MC cost
+is exactly proportional to the walker count, so it is timed on a bounded walker sample and
+scaled), and the CPU oracle (restated reference algorithm, all host cores) on a bounded sample.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NINT_WORKLOAD = "h2o_26"
+WALKERS = 1 << 26
+NBLOCKS = 16
+A_ZV = 1.8
+SIGMA_TARGET = 1e-6
+
+
+def _workload():
+    from slater_stoch_gb300 import basis, configs
+    b = configs.h2o_26(ng0=20)
+    q = basis.build_mapping(b.n)
+    return b, q
+
+
+# ------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 3 + i and r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline: the oracle (restated reference) on bounded samples of the workload
+# ------------------------------------------------------------------------------------------
+def cpu_baseline(b, q, budget_s: float = 20.0):
+    from oracle import binding as O
+    ob = O.OracleBasis(b)
+    nint = len(q[0])
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    # analytic stage: a random subset of quartets, scaled by primitive-quartet count
+    total_prims = O.count_primitive_quartets(ob, q)
+    t = time.perf_counter()
+    pre = O.precond(ob, cores)
+    t_pre = time.perf_counter() - t
+    sel = rng.choice(nint, size=64, replace=False)
+    sub = tuple(np.ascontiguousarray(a[sel]) for a in q)
+    sub_prims = O.count_primitive_quartets(ob, sub)
+    t = time.perf_counter()
+    O.gauss_eri(ob, sub, pre, cores)
+    t_sub = time.perf_counter() - t
+    t_analytic = t_pre + t_sub * total_prims / sub_prims
+    # MC stage: faithful estimator (reference algorithm) on a bounded walker sample
+    npts = 40 * 100
+    r = np.random.default_rng(1)
+    r1 = r.standard_normal((npts, 3))
+    r2 = r.standard_normal((npts, 3))
+    t = time.perf_counter()
+    O.zvmc_faithful(ob, q, A_ZV, r1, r2, 1, npts, "ref32", nthreads=cores)
+    t_mc_sample = time.perf_counter() - t
+    t_mc = t_mc_sample * WALKERS / npts
+    job = t_analytic + t_mc
+    return {
+        "value": nint / job, "unit": "ERIs/s", "cores": cores, "kind": "port",
+        "sample": (f"oracle (C restatement of the reference, OpenMP {cores} threads): Schwarz diagonal "
+                   f"in full ({t_pre:.1f}s) + 64 random quartets ({sub_prims:.3g} of {total_prims:.3g} "
+                   f"primitive quartets, {t_sub:.1f}s) scaled by primitive-quartet count; faithful "
+                   f"ZV-MC (ref32 casts) on {npts} walkers ({t_mc_sample:.1f}s) scaled to {WALKERS}"),
+        "job_seconds_estimated": job, "analytic_s": t_analytic, "mc_s": t_mc,
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    b, q = _workload()
+    cb = cpu_baseline(b, q)
+    line = {
+        "impl": "reference", "metric": "unique ERIs/s at sigma<=1e-6 Ha (two-electron ZV-MC job)",
+        "value": cb["value"], "unit": "ERIs/s", "n_gpus": 0, "steps": 1, "warmup": 0,
+        "ms_per_step": cb["job_seconds_estimated"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "h2o_26: H2O 26 STOs, 20-Gaussian fits, 61776 ERIs, 2^26 walker pairs",
+                   "estimator": "faithful (reference), ref32 casts"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": "ERIs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def fp64_peak_tflops(torch):
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    bm = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, bm)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(3):
+        e0.record()
+        torch.matmul(a, bm)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--walkers", type=int, default=WALKERS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    from slater_stoch_gb300 import api
+    from slater_stoch_gb300.perfmodel import eri_fp64_flops
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    b, q = _workload()
+    nint = len(q[0])
+    npts = args.walkers // NBLOCKS
+    ctx = api.Context(local)
+    ctx.set_basis(b)
+    ctx.set_quartets(*q)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    seed = 1 + rank
+
+    def job():
+        ctx.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=False)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        job()
+    barrier()
+    times = []
+    l0 = ctx.launches
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            job()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    launches = (ctx.launches - l0) // max(args.steps, 1)
+    max_sigma = ctx.max_sigma
+    tmax = torch.tensor([sum(times)], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    ms_step = float(tmax.item()) / args.steps
+    value = world * nint / (ms_step * 1e-3)
+
+    # end-to-end through the C ABI with host buffers: upload basis + quartets, copy results back
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 2))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        c2 = api.Context(local)
+        c2.set_basis(b)
+        c2.set_quartets(*q)
+        eri, sig = c2.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=True)
+        e2e_times.append(time.perf_counter() - t)
+        c2.close()
+    h2d = sum(a.nbytes for a in ctx._basis_arrays) + 4 * 4 * nint
+    d2h = 2 * 8 * nint
+
+    # stage split of one job (events on the library stream)
+    ctx.invalidate()
+    torch.cuda.synchronize()
+    s0, s1, s2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    s0.record(stream)
+    ctx.gauss_eri(copy=False)
+    s1.record(stream)
+    ctx.zvmc(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", copy=False)
+    s2.record(stream)
+    s2.synchronize()
+    t_analytic = s0.elapsed_time(s1) * 1e-3
+    t_mc = s1.elapsed_time(s2) * 1e-3
+
+    # FP64 plain path: faithful per-pair estimator in FP64; MC time is linear in walkers
+    plain_npts = 40 * 8192
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.zvmc(A_ZV, seed, 40 * 256, 1, "faithful", "fp64", copy=False)  # warm
+    p0.record(stream)
+    ctx.zvmc(A_ZV, seed, plain_npts, 1, "faithful", "fp64", copy=False)
+    p1.record(stream)
+    p1.synchronize()
+    t_plain_mc = p0.elapsed_time(p1) * 1e-3 * args.walkers / plain_npts
+    plain_value = nint / (t_analytic + t_plain_mc)
+
+    from slater_stoch_gb300.perfmodel import primitive_quartets
+    nprim = primitive_quartets(b, q)
+    flops = eri_fp64_flops(b, q)
+    peak64 = fp64_peak_tflops(torch)
+    achieved = flops / t_analytic / 1e12 if flops else None
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                "frac": achieved / peak64 if (peak64 and achieved) else None, "traffic": None,
+                "kernel": "eri_kernel (analytic FP64 Gaussian-fit ERIs, all launches of one job)",
+                "peak_source": "measured in this run: torch float64 matmul 4096^3 (FP64 peak is not "
+                               "in MEASURED_PEAKS.json)",
+                "units": f"{nprim:.4g} primitive quartets x FP64 flops per primitive quartet"}
+
+    if rank == 0:
+        lat = sorted(times)
+        line = {
+            "metric": "unique ERIs/s at sigma<=1e-6 Ha (two-electron ZV-MC job), split-BF16 vs FP64 plain",
+            "value": value, "unit": "ERIs/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 analytic + bf16x3 (fp32 accumulate) MC", "data": "synthetic",
+            "config": {"workload": "h2o_26: H2O O(0,0,0) H(0,+-1.4305,1.1093) bohr, 26 STOs, 20-Gaussian fits, "
+                                   "61776 unique ERIs, 2^26 walker pairs",
+                       "walkers": args.walkers, "blocks": NBLOCKS, "estimator": "shared-walker, split-BF16",
+                       "max_sigma_Ha": max_sigma, "sigma_target_Ha": SIGMA_TARGET,
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "stages_s": {"analytic": t_analytic, "mc_split_bf16": t_mc},
+            "fp64_plain": {"value": plain_value, "unit": "ERIs/s", "analytic_s": t_analytic,
+                           "mc_s_scaled": t_plain_mc, "measured_walkers": plain_npts,
+                           "speedup_split_bf16_vs_fp64_plain": value / world / plain_value},
+            "e2e": {"value": world * nint / statistics.median(e2e_times), "unit": "ERIs/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "clocks": clk.summary(),
+            "wall_s_timed": t_wall,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            cb = cpu_baseline(b, q)
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

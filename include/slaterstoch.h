@@ -1,0 +1,141 @@
+/*
+ * slaterstoch.h -- C ABI of libslaterstoch.so, the GB300 (sm_103a) implementation of the
+ * two-electron path of scemama/slater_stoch: analytic ERIs of each STO's Gaussian fit,
+ * the zero-variance Monte Carlo (ZV-MC) STO-minus-fit correction, and the PSD cleanup.
+ *
+ * Conventions (match the reference's Fortran data so a driver can pass its arrays as is):
+ *  - arrays are column-major Fortran arrays: center(3,n), npower(3,n), c_gauss(ld,n,2),
+ *    g_gauss(ld,n); quartet indices is/js/ks/ls are 1-based and (is,ks) is electron 1,
+ *    (js,ls) electron 2, i.e. the value is (ik|jl) = <ij|kl> (src/build_mapping_ijkl.F90:24-43);
+ *  - host arrays are caller-owned and read/written before the call returns;
+ *  - every call returns 0 (SS_OK) or a negative SS_ERR_* code and never exits the process
+ *    (the reference's `stop` statements become error codes); ss_last_error() gives a message;
+ *  - one ss_ctx per host thread; a context owns all device memory it allocates.
+ */
+#ifndef SLATERSTOCH_H
+#define SLATERSTOCH_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SS_OK 0
+#define SS_ERR_ARG (-1)        /* invalid argument (sizes, indices, npts not a multiple of 40) */
+#define SS_ERR_STATE (-2)      /* call out of order (e.g. no basis set) */
+#define SS_ERR_CUDA (-3)       /* a CUDA runtime call failed */
+#define SS_ERR_NOMEM (-4)      /* device allocation failed or exceeds the context's HBM budget */
+#define SS_ERR_UNSUPPORTED (-5) /* input outside the kernels' limits (angular momentum, i_type 3) */
+#define SS_ERR_TIMEOUT (-6)    /* a bounded device wait gave up */
+#define SS_ERR_NUMERIC (-7)    /* non-finite result detected (e.g. Taylor series did not converge) */
+
+#define SS_EST_FAITHFUL 0      /* per-pair ZV map, src/two_e_slater.F90:401-454 */
+#define SS_EST_SHARED 1        /* one walker set for all pairs (tensor-core contraction) */
+
+#define SS_PREC_FP64 0         /* FP64 arithmetic (src/two_e_slater.F90:443,447 variant) */
+#define SS_PREC_REF32 1        /* the reference's FP32 casts of weight and 1/r12 (:442,:446) */
+#define SS_PREC_SPLIT_BF16 2   /* shared estimator: BF16 hi+lo, 3 products, FP32 accumulate */
+
+#define SS_LAYOUT_REF_N2 0     /* svd_clean's n^2 x n^2 <ij|kl> matrix (src/svd_clean.F90:97-130) */
+#define SS_LAYOUT_PACKED_PAIR 1 /* packed Coulomb metric M[(ik),(jl)] = (ik|jl) */
+
+typedef struct ss_ctx ss_ctx;
+
+/* Create a context on CUDA device `device`; hbm_budget bytes caps its device allocations
+ * (0 = no cap).  Returns NULL on failure (see ss_last_error()). */
+ss_ctx* ss_create(int device, size_t hbm_budget);
+void ss_destroy(ss_ctx* ctx);
+const char* ss_strerror(int code);
+const char* ss_last_error(void);
+/* number of kernels this context has launched (diagnostics) */
+int64_t ss_launch_count(const ss_ctx* ctx);
+
+/* Replaces the basis arrays of module common_data (src/common_data.F90:37-52) as built by
+ * build_gaussian_expansion_of_orbitals (src/build_gaussian_expansion_of_orbitals.F90:1-473).
+ * center(3,n) bohr; npower(3,n); n_sto(n); i_type(n) in {1,2}; n_gauss(n) <= ld;
+ * c_gauss(ld,n,2); g_gauss(ld,n); g_slater(n) = zeta. */
+int ss_basis_set(ss_ctx* ctx, int nbasis, const double* center, const int* npower,
+                 const int* n_sto, const int* i_type, const int* n_gauss, const double* c_gauss,
+                 int ld, const double* g_gauss, const double* g_slater);
+
+/* Replaces is/js/ks/ls of common_data built by build_mapping_ijkl (src/build_mapping_ijkl.F90). */
+int ss_quartets_set(ss_ctx* ctx, int64_t nint, const int32_t* is, const int32_t* js,
+                    const int32_t* ks, const int32_t* ls);
+
+/* Schwarz diagonal precond(i,k) = (ik|ik), n x n column-major, i >= k filled and mirrored
+ * (replaces src/two_e_slater.F90:230-239). */
+int ss_precond(ss_ctx* ctx, double* precond);
+
+/* Analytic (ik|jl) of the Gaussian fits for every quartet, with the reference's Schwarz
+ * screening and diagonal reuse (replaces the gauss_ijkl loop, src/two_e_slater.F90:264-284,
+ * and gauss_ijkl itself, src/gauss_ijkl.F90:51).  out may be NULL (result kept on device);
+ * n_removed (may be NULL) receives the Schwarz-removed count (:253-262). */
+int ss_gauss_eri(ss_ctx* ctx, double* out, int64_t* n_removed);
+
+/* ZV-MC correction <ij|kl>_STO - <ij|kl>_fit (replaces src/two_e_slater.F90:386-496).
+ * Walkers come from a counter-based Philox4x32-10 stream keyed by `seed`.
+ * estimator: SS_EST_FAITHFUL (precision FP64 or REF32) or SS_EST_SHARED (FP64 or SPLIT_BF16).
+ * nblocks blocks of samples_per_block samples (faithful: a multiple of 40, src/two_e_slater.F90:148).
+ * sigma_target > 0 stops after the first block boundary where max sigma <= target (needs >= 2
+ * blocks done).  mean/sigma: nint each (may be NULL; kept on device). */
+int ss_zvmc(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
+            int estimator, int precision, double sigma_target, double* mean, double* sigma);
+
+/* Faithful estimator on caller-supplied walkers (the parity hook): r1, r2 are (3,S) walker-major
+ * standard normals, S = nblocks*npts, as drawn by draw_configuration (src/draw_configuration.F90). */
+int ss_zvmc_walkers(ss_ctx* ctx, double a_zv, const double* r1, const double* r2, int64_t npts,
+                    int nblocks, int precision, double* mean, double* sigma);
+
+/* The walkers the faithful estimator draws for (seed, first sample, S): r1, r2 (3,S). */
+int ss_draw_walkers(ss_ctx* ctx, uint64_t seed, int64_t first, int64_t S, double* r1, double* r2);
+
+/* Shared-walker estimator: the sample points u1, u2 (3,S) and weights w (S) it draws for
+ * (seed, first sample), so a checker can recompute the estimator in FP64. */
+int ss_shared_samples(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t first, int64_t S,
+                      double* u1, double* u2, double* w);
+
+/* Final ERIs = analytic + MC mean (src/two_e_slater.F90:558-564); out nint. */
+int ss_combine(ss_ctx* ctx, double* out);
+
+/* The whole two-electron job of the reference driver on the resident basis and quartets
+ * (src/two_e_slater.F90:219-564: Schwarz diagonal, analytic ERIs, ZV-MC blocks, merge),
+ * recomputed from scratch.  Results stay on the device; fetch them with ss_combine /
+ * ss_gauss_eri / the mean/sigma of a later ss_zvmc call.  eri/sigma (nint, may be NULL)
+ * receive the merged integrals and their MC error. */
+int ss_two_e_job(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
+                 int estimator, int precision, double sigma_target, double* eri, double* sigma);
+
+/* Drop cached device results (Schwarz diagonal, analytic ERIs, MC sums); inputs stay. */
+int ss_invalidate(ss_ctx* ctx);
+
+/* Largest MC error of the last ZV-MC run, and the number of blocks it used. */
+double ss_mc_max_sigma(const ss_ctx* ctx);
+int ss_mc_blocks_done(const ss_ctx* ctx);
+
+/* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+void* ss_stream(ss_ctx* ctx);
+
+/* The shared estimator's tensor-core contraction on caller data (no reference counterpart;
+ * it replaces the quartet loop of src/two_e_slater.F90:424-453 for the shared estimator):
+ * C(P,P) = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with A*, B* (P,K) row-major BF16 bit
+ * patterns, K a positive multiple of 64, C row-major FP32, FP32 accumulation per K slice of
+ * ksplit (0 = automatic) summed in FP64. */
+int ss_split_bf16_gemm(ss_ctx* ctx, int P, int64_t K, const uint16_t* a_hi, const uint16_t* a_lo,
+                       const uint16_t* b_hi, const uint16_t* b_lo, int ksplit, float* c);
+
+/* PSD cleanup by randomized SVD deflation (replaces svd_clean, src/svd_clean.F90:1-426).
+ * moy (nint) in/out; rank, q as in src/two_e_slater.F90:565-567 (oversample added to rank);
+ * seed drives the Gaussian test matrices.  n_removed receives the removed negative components. */
+int ss_psd_clean(ss_ctx* ctx, double* moy, int layout, int rank, int oversample, int q,
+                 uint64_t seed, int* n_removed);
+
+/* Lowest m eigenpairs of the ERI matrix in `layout` by Davidson with FP64 Rayleigh-Ritz
+ * (follows src/davidson.F90:1-158).  evals (m), evecs (N x m column-major) may be NULL. */
+int ss_davidson(ss_ctx* ctx, const double* moy, int layout, int m, double tol, int max_iter,
+                double* evals, double* evecs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

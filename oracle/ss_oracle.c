@@ -1,0 +1,1014 @@
+/*
+ * ss_oracle.c -- CPU oracle for the two-electron ZV-MC path (TEST INFRASTRUCTURE).
+ *
+ * A plain-C restatement of the reference's FP64 algorithms, used only as the
+ * checker of the CUDA path (tests/, the smoke check) and as the CPU baseline
+ * of bench.py.  Each function cites the reference file:line it follows.
+ * Built with -ffp-contract=off so no fused multiply-adds change the rounding
+ * of the reference's expressions.
+ *
+ * Parity status: the reference has no tests or golden outputs and cannot be
+ * compiled here (Fortran, no compiler); this oracle is pinned by analytic
+ * known-answer tests (see tests/test_oracle_kat.py).
+ *
+ * Known, documented deviations from the reference's arithmetic:
+ *  - fact(n) (src/fact.F90:1-27) returns exp(logfact(n)) on the first call
+ *    for a new n and the memoised product afterwards; the oracle always uses
+ *    the memoised product memo(i) = memo(i-1)*i (the steady state).
+ */
+#include "ss_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MAXD 160 /* polynomial scratch; the reference uses 0:511 (max_dim) */
+static const double THRESH = 1.e-15;
+static const double PI_5_2 = 34.9868366552; /* 12-digit constant, src/general_primitive_integral.F90:25 */
+
+/* ------------------------------------------------------------------ */
+/* factorials (src/fact.F90:1-34, src/logfact.F90:1-29)                */
+/* ------------------------------------------------------------------ */
+static double g_fact[101];
+static double g_logfact[101];
+static double g_binom[16][16];
+static int g_init = 0;
+
+static void init_tables(void) {
+  if (g_init) return;
+  g_fact[0] = 1.0;
+  g_fact[1] = 1.0;
+  for (int i = 2; i <= 100; i++) g_fact[i] = g_fact[i - 1] * (double)i;
+  g_logfact[0] = 0.0;
+  g_logfact[1] = 0.0;
+  for (int i = 2; i <= 100; i++) g_logfact[i] = g_logfact[i - 1] + log((double)i);
+  /* binom_func memo (src/binom_func.F90:14-21) */
+  for (int k = 0; k <= 15; k++)
+    for (int l = 0; l <= 15; l++) {
+      double lf_kl = (k - l) < 2 ? 0.0 : g_logfact[k - l];
+      g_binom[k][l] = exp(g_logfact[k] - g_logfact[l] - lf_kl);
+    }
+  g_init = 1;
+}
+
+static double fact(int n) { return n < 2 ? 1.0 : g_fact[n]; }
+static double fact_inv(int n) { return 1.0 / fact(n); }
+
+static double logfact(int n) {
+  if (n < 2) return 0.0;
+  if (n <= 100) return g_logfact[n];
+  double v = g_logfact[100];
+  for (int i = 101; i <= n; i++) v += log((double)i);
+  return v;
+}
+
+static double binom_func(int i, int j) {
+  if (i <= 15 && j <= 15 && i >= 0 && j >= 0) return g_binom[i][j];
+  return exp(logfact(i) - logfact(j) - logfact(i - j));
+}
+
+/* ------------------------------------------------------------------ */
+/* polynomial helpers                                                  */
+/* ------------------------------------------------------------------ */
+/* D(t) += B(t)*C(t) ; nd = highest nonzero index (src/multiply_poly.F90:1-40) */
+static void multiply_poly(const double *b, int nb, const double *c, int nc, double *d, int *nd) {
+  if (nb < 0 || nc < 0) return;
+  int ndtmp = nb + nc;
+  for (int ic = 0; ic <= nc; ic++) d[ic] = d[ic] + c[ic] * b[0];
+  for (int ib = 1; ib <= nb; ib++) {
+    d[ib] = d[ib] + c[0] * b[ib];
+    for (int ic = 1; ic <= nc; ic++) d[ib + ic] = d[ib + ic] + c[ic] * b[ib];
+  }
+  int k;
+  for (k = ndtmp; k >= 0; k--)
+    if (d[k] != 0.0) break;
+  *nd = k;
+}
+
+/* D(t) += cst*B(t) (src/add_poly_multiply.F90:1-28) */
+static void add_poly_multiply(const double *b, int nb, double cst, double *d, int *nd) {
+  *nd = (*nd > nb) ? *nd : nb;
+  if (*nd != -1) {
+    for (int ib = 0; ib <= nb; ib++) d[ib] = d[ib] + cst * b[ib];
+    while (d[*nd] == 0.0) {
+      (*nd)--;
+      if (*nd < 0) break;
+    }
+  }
+}
+
+/* (x - x_A)^a expanded around x_P (src/give_explicit_poly_and_gaussian.F90:86-220) */
+static void recentered_poly(double *P, double x_A, double x_P, int a) {
+  double pw[MAXD];
+  if (a < 0) return;
+  pw[0] = 1.0;
+  pw[1] = x_P - x_A;
+  switch (a) {
+    case 0: P[0] = pw[0]; return;
+    case 1: P[0] = pw[1]; P[1] = pw[0]; return;
+    case 2:
+      pw[2] = pw[1] * pw[1];
+      P[0] = pw[2]; P[1] = 2.0 * pw[1]; P[2] = pw[0];
+      return;
+    case 3:
+      pw[2] = pw[1] * pw[1]; pw[3] = pw[2] * pw[1];
+      P[0] = pw[3]; P[1] = 3.0 * pw[2]; P[2] = 3.0 * pw[1]; P[3] = pw[0];
+      return;
+    case 4:
+      pw[2] = pw[1] * pw[1]; pw[3] = pw[2] * pw[1]; pw[4] = pw[2] * pw[2];
+      P[0] = pw[4]; P[1] = 4.0 * pw[3]; P[2] = 6.0 * pw[2]; P[3] = 4.0 * pw[1]; P[4] = pw[0];
+      return;
+    default: break;
+  }
+  for (int i = 2; i <= a; i++) pw[i] = pw[i - 1] * pw[1];
+  if (a <= 8) {
+    /* cases 5..8: exact integer binomials times powers */
+    static const double bin[9][9] = {
+        {1}, {1, 1}, {1, 2, 1}, {1, 3, 3, 1}, {1, 4, 6, 4, 1}, {1, 5, 10, 10, 5, 1},
+        {1, 6, 15, 20, 15, 6, 1}, {1, 7, 21, 35, 35, 21, 7, 1}, {1, 8, 28, 56, 70, 56, 28, 8, 1}};
+    P[0] = pw[a];
+    for (int i = 1; i <= a; i++) P[i] = bin[a][i] * pw[a - i];
+    return;
+  }
+  P[0] = pw[a];
+  for (int i = 1; i <= a; i++) P[i] = binom_func(a, a - i) * pw[a - i];
+}
+
+/* 3D Gaussian product (src/gaussian_product.F90:1-33); returns 0 if exponent > 40 */
+static void gaussian_product(double a, const double *xa, double b, const double *xb, double *k,
+                             double *p, double *xp) {
+  *p = a + b;
+  double p_inv = 1.0 / (a + b);
+  double ab = a * b;
+  double xab0 = xa[0] - xb[0], xab1 = xa[1] - xb[1], xab2 = xa[2] - xb[2];
+  ab = ab * p_inv;
+  double kk = ab * (xab0 * xab0 + xab1 * xab1 + xab2 * xab2);
+  if (kk > 40.0) {
+    *k = 0.0;
+    xp[0] = xp[1] = xp[2] = 0.0; /* left unset by the reference; never used */
+    return;
+  }
+  *k = exp(-kk);
+  xp[0] = (a * xa[0] + b * xb[0]) * p_inv;
+  xp[1] = (a * xa[1] + b * xb[1]) * p_inv;
+  xp[2] = (a * xa[2] + b * xb[2]) * p_inv;
+}
+
+/* (src/give_explicit_poly_and_gaussian.F90:1-84); P_new[axis*MAXD + i] */
+static void give_explicit_poly_and_gaussian(double *P_new, double *P_center, double *p,
+                                            double *fact_k, int *iorder, double alpha, double beta,
+                                            const int *a, const int *b, const double *A,
+                                            const double *B) {
+  iorder[0] = iorder[1] = iorder[2] = 0;
+  P_new[0] = P_new[MAXD] = P_new[2 * MAXD] = 0.0;
+  gaussian_product(alpha, A, beta, B, fact_k, p, P_center);
+  if (*fact_k < THRESH) {
+    *fact_k = 0.0;
+    return;
+  }
+  for (int ax = 0; ax < 3; ax++) {
+    double Pa[MAXD], Pb[MAXD];
+    recentered_poly(Pa, A[ax], P_center[ax], a[ax]);
+    recentered_poly(Pb, B[ax], P_center[ax], b[ax]);
+    iorder[ax] = a[ax] + b[ax];
+    double *Pn = P_new + ax * MAXD;
+    for (int i = 0; i <= iorder[ax]; i++) Pn[i] = 0.0;
+    int n_new = 0;
+    multiply_poly(Pa, a[ax], Pb, b[ax], Pn, &n_new);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Rys-like polynomial recursions in t (src/I_x1_pol_mult*.F90, I_x2_pol_mult.F90) */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  double B10[3], B01[3], B00[3], C00[3], D00[3];
+} rec_coef;
+
+static void I_x2_pol_mult(int c, const rec_coef *R, double *d, int *nd, int dim);
+static void I_x1_pol_mult_a1(int c, const rec_coef *R, double *d, int *nd, int n_pt_in);
+static void I_x1_pol_mult_a2(int c, const rec_coef *R, double *d, int *nd, int n_pt_in);
+static void I_x1_pol_mult_recurs(int a, int c, const rec_coef *R, double *d, int *nd, int n_pt_in);
+
+/* (src/I_x2_pol_mult.F90:1-84) */
+static void I_x2_pol_mult(int c, const rec_coef *R, double *d, int *nd, int dim) {
+  double X[MAXD], Y[MAXD];
+  int nx, ny;
+  if (c == 0) {
+    *nd = 0;
+    d[0] = 1.0;
+    return;
+  }
+  if (c < 0) {
+    *nd = -1;
+    return;
+  }
+  if (c == 1) {
+    *nd = 2;
+    d[0] = R->D00[0]; d[1] = R->D00[1]; d[2] = R->D00[2];
+    return;
+  }
+  if (c == 2) {
+    *nd = 2;
+    d[0] = R->B01[0]; d[1] = R->B01[1]; d[2] = R->B01[2];
+    ny = 2;
+    Y[0] = R->D00[0]; Y[1] = R->D00[1]; Y[2] = R->D00[2];
+    multiply_poly(Y, ny, R->D00, 2, d, nd);
+    return;
+  }
+  for (int ix = 0; ix <= c + c; ix++) X[ix] = 0.0;
+  nx = 0;
+  I_x2_pol_mult(c - 2, R, X, &nx, dim);
+  for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (double)(c - 1);
+  multiply_poly(X, nx, R->B01, 2, d, nd);
+  ny = 0;
+  for (int ix = 0; ix <= c + c; ix++) Y[ix] = 0.0;
+  I_x2_pol_mult(c - 1, R, Y, &ny, dim);
+  multiply_poly(Y, ny, R->D00, 2, d, nd);
+}
+
+/* (src/I_x1_pol_mult_a1.F90:1-59) */
+static void I_x1_pol_mult_a1(int c, const rec_coef *R, double *d, int *nd, int n_pt_in) {
+  double X[MAXD], Y[MAXD];
+  int nx, ny;
+  if (c < 0 || *nd < 0) {
+    *nd = -1;
+    return;
+  }
+  nx = *nd;
+  for (int ix = 0; ix <= n_pt_in; ix++) X[ix] = 0.0;
+  I_x2_pol_mult(c - 1, R, X, &nx, n_pt_in);
+  if (c > 1)
+    for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (double)c;
+  multiply_poly(X, nx, R->B00, 2, d, nd);
+  ny = 0;
+  for (int ix = 0; ix <= n_pt_in; ix++) Y[ix] = 0.0;
+  I_x2_pol_mult(c, R, Y, &ny, n_pt_in);
+  multiply_poly(Y, ny, R->C00, 2, d, nd);
+}
+
+/* (src/I_x1_pol_mult_a2.F90:1-61) */
+static void I_x1_pol_mult_a2(int c, const rec_coef *R, double *d, int *nd, int n_pt_in) {
+  double X[MAXD], Y[MAXD];
+  int nx, ny;
+  for (int ix = 0; ix <= n_pt_in; ix++) X[ix] = 0.0;
+  nx = 0;
+  I_x2_pol_mult(c, R, X, &nx, n_pt_in);
+  multiply_poly(X, nx, R->B10, 2, d, nd);
+  nx = *nd;
+  for (int ix = 0; ix <= n_pt_in; ix++) X[ix] = 0.0;
+  I_x1_pol_mult_a1(c - 1, R, X, &nx, n_pt_in);
+  if (c > 1)
+    for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (double)c;
+  multiply_poly(X, nx, R->B00, 2, d, nd);
+  ny = 0;
+  for (int ix = 0; ix <= n_pt_in; ix++) Y[ix] = 0.0;
+  I_x1_pol_mult_a1(c, R, Y, &ny, n_pt_in);
+  multiply_poly(Y, ny, R->C00, 2, d, nd);
+}
+
+/* (src/I_x1_pol_mult_recurs.F90:1-80) */
+static void I_x1_pol_mult_recurs(int a, int c, const rec_coef *R, double *d, int *nd, int n_pt_in) {
+  double X[MAXD], Y[MAXD];
+  int nx, ny;
+  for (int ix = 0; ix <= n_pt_in; ix++) X[ix] = 0.0;
+  nx = 0;
+  if (a == 3)
+    I_x1_pol_mult_a1(c, R, X, &nx, n_pt_in);
+  else if (a == 4)
+    I_x1_pol_mult_a2(c, R, X, &nx, n_pt_in);
+  else
+    I_x1_pol_mult_recurs(a - 2, c, R, X, &nx, n_pt_in);
+  for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (double)(a - 1);
+  multiply_poly(X, nx, R->B10, 2, d, nd);
+  nx = *nd;
+  for (int ix = 0; ix <= n_pt_in; ix++) X[ix] = 0.0;
+  if (c > 0) {
+    if (a == 3)
+      I_x1_pol_mult_a2(c - 1, R, X, &nx, n_pt_in);
+    else
+      I_x1_pol_mult_recurs(a - 1, c - 1, R, X, &nx, n_pt_in);
+    if (c > 1)
+      for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (double)c;
+    multiply_poly(X, nx, R->B00, 2, d, nd);
+  }
+  ny = 0;
+  for (int ix = 0; ix <= n_pt_in; ix++) Y[ix] = 0.0;
+  if (a == 3)
+    I_x1_pol_mult_a2(c, R, Y, &ny, n_pt_in);
+  else
+    I_x1_pol_mult_recurs(a - 1, c, R, Y, &ny, n_pt_in);
+  multiply_poly(Y, ny, R->C00, 2, d, nd);
+}
+
+/* (src/I_x1_pol_mult.F90:1-47) */
+static void I_x1_pol_mult(int a, int c, const rec_coef *R, double *d, int *nd, int n_pt_in) {
+  if (c >= 0 && *nd >= 0) {
+    if (a == 1)
+      I_x1_pol_mult_a1(c, R, d, nd, n_pt_in);
+    else if (a == 2)
+      I_x1_pol_mult_a2(c, R, d, nd, n_pt_in);
+    else if (a > 2)
+      I_x1_pol_mult_recurs(a, c, R, d, nd, n_pt_in);
+    else {
+      if (c == 0) {
+        *nd = 0;
+        d[0] = 1.0;
+        return;
+      }
+      I_x2_pol_mult(c, R, d, nd, n_pt_in);
+    }
+  } else {
+    *nd = -1;
+  }
+}
+
+/* (src/give_polynom_mult_center_x.F90:1-74) */
+static void give_polynom_mult_center_x(double P_center, double Q_center, int a_x, int d_x, double p,
+                                       double q, int n_pt_in, double pq_inv, double pq_inv_2,
+                                       double p10_1, double p01_1, double p10_2, double p01_2,
+                                       double *d, int *n_pt_out) {
+  rec_coef R;
+  R.B10[0] = p10_1; R.B10[1] = 0.0; R.B10[2] = -p10_2;
+  R.B01[0] = p01_1; R.B01[1] = 0.0; R.B01[2] = -p01_2;
+  R.B00[0] = 0.0; R.B00[1] = 0.0; R.B00[2] = pq_inv;
+  for (int i = 0; i <= n_pt_in; i++) d[i] = 0.0;
+  int n_pt1 = n_pt_in;
+  R.C00[0] = 0.0; R.C00[1] = 0.0; R.C00[2] = -q * (P_center - Q_center) * pq_inv_2;
+  R.D00[0] = 0.0; R.D00[1] = 0.0; R.D00[2] = -p * (Q_center - P_center) * pq_inv_2;
+  I_x1_pol_mult(a_x, d_x, &R, d, &n_pt1, n_pt_in);
+  *n_pt_out = n_pt1;
+  if (n_pt1 < 0) {
+    *n_pt_out = -1;
+    for (int i = 0; i <= n_pt_in; i++) d[i] = 0.0;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Boys-type integrals                                                 */
+/* ------------------------------------------------------------------ */
+/* Taylor series of F_n for rho < 1 (src/rint1.F90:1-59); NaN if not converged */
+static double rint1(int n, double rho) {
+  const double eps = 1.e-15;
+  double r, rho_tmp = 1.0, diff = 0.0;
+  if (n < 50) {
+    r = 1.0 / (double)(n + n + 1);
+    for (int k = 1; k <= 20; k++) {
+      rho_tmp = -rho_tmp * rho;
+      diff = rho_tmp * fact_inv(k) * (1.0 / (double)(2 * (k + n) + 1));
+      r = r + diff;
+      if (fabs(diff) > eps) continue;
+      return r;
+    }
+  } else {
+    r = 1.0 / (double)(n + n + 1);
+    for (int k = 1; k <= 20; k++) {
+      rho_tmp = -rho_tmp * rho;
+      diff = rho_tmp * fact_inv(k) / (double)(2 * (k + n) + 1);
+      r = r + diff;
+      if (fabs(diff) > eps) continue;
+      return r;
+    }
+  }
+  return NAN; /* the reference stops the program here (src/rint1.F90:56-58) */
+}
+
+/* (src/hermite.F90:1-24) */
+static double hermite(int n, double x) {
+  double h0 = 1.0, h1, h2 = 0.0;
+  if (n == 0) return h0;
+  h1 = x + x;
+  if (n == 1) return h1;
+  for (int k = 1; k <= n - 1; k++) {
+    h2 = (x + x) * h1 - (double)(k + k) * h0;
+    h0 = h1;
+    h1 = h2;
+  }
+  return h2;
+}
+
+static double powi(double x, int k) { /* x**k, binary exponentiation */
+  double r = 1.0, b = x;
+  while (k > 0) {
+    if (k & 1) r *= b;
+    b *= b;
+    k >>= 1;
+  }
+  return r;
+}
+
+/* (src/rint_large_n.F90:1-29) */
+static double rint_large_n(int n, double rho) {
+  double u = sqrt(rho), accu = 0.0, eps = 1.0;
+  int k = 0;
+  while (eps > 1.e-15 && k < 200) {
+    double t1 = 1.0;
+    for (int l = 0; l <= k; l++) t1 = t1 * ((double)(n + n + l) + 1.0);
+    double t2 = 0.0;
+    for (int l = 0; l <= k; l++) t2 = t2 + ((l & 1) ? -1.0 : 1.0) / (fact(l + 1) * fact(k - l));
+    double alpha_k = t2 * fact(k + 1) * fact(k) * ((k & 1) ? -1.0 : 1.0);
+    alpha_k = alpha_k / t1;
+    double rajout = ((k & 1) ? -1.0 : 1.0) * powi(u, k) * hermite(k, u) * alpha_k / fact(k);
+    accu = accu + rajout;
+    eps = fabs(rajout) / accu;
+    k = k + 1;
+  }
+  return exp(-rho) * accu;
+}
+
+double orc_rint_sum(int n_pt_out, double rho, const double *d1) {
+  init_tables();
+  const double sqpi = sqrt(M_PI);
+  double r;
+  if (rho < 1.0) {
+    if (rho == 0.0) {
+      r = d1[0];
+    } else {
+      double u_inv = 1.0 / sqrt(rho);
+      double u = rho * u_inv;
+      r = 0.5 * u_inv * sqpi * erf(u) * d1[0];
+    }
+    for (int i = 2; i <= n_pt_out; i += 2) r = r + d1[i] * rint1(i >> 1, rho);
+  } else {
+    double v = (rho > 80.0) ? 0.0 : exp(-rho);
+    double u_inv = 1.0 / sqrt(rho);
+    double u = rho * u_inv;
+    double two_rho_inv = 0.5 * u_inv * u_inv;
+    double val0 = 0.5 * u_inv * sqpi * erf(u);
+    r = val0 * d1[0];
+    double rint_tmp = (val0 - v) * two_rho_inv;
+    double di = 3.0;
+    int top = n_pt_out < 40 ? n_pt_out : 40;
+    for (int i = 2; i <= top; i += 2) {
+      r = r + d1[i] * rint_tmp;
+      rint_tmp = (rint_tmp * di - v) * two_rho_inv;
+      di = di + 2.0;
+    }
+    for (int i = 42; i <= n_pt_out; i += 2) r = r + d1[i] * rint_large_n(i >> 1, rho);
+  }
+  return r;
+}
+
+/* (src/rint.F90:1-63) */
+double orc_rint(int n, double rho) {
+  init_tables();
+  const double sqpi = sqrt(M_PI);
+  if (n == 0) {
+    if (rho == 0.0) return 1.0;
+    double u_inv = 1.0 / sqrt(rho);
+    double u = rho * u_inv;
+    return 0.5 * u_inv * sqpi * erf(u);
+  }
+  if (rho < 1.0) return rint1(n, rho);
+  if (n <= 20) {
+    double u_inv = 1.0 / sqrt(rho);
+    double v = (rho > 80.0) ? 0.0 : exp(-rho);
+    double u = rho * u_inv;
+    double two_rho_inv = 0.5 * u_inv * u_inv;
+    double val0 = 0.5 * u_inv * sqpi * erf(u);
+    double r = (val0 - v) * two_rho_inv;
+    for (int k = 2; k <= n; k++) r = (r * (double)(k + k - 1) - v) * two_rho_inv;
+    return r;
+  }
+  return rint_large_n(n, rho);
+}
+
+/* ------------------------------------------------------------------ */
+/* primitive ERI                                                       */
+/* ------------------------------------------------------------------ */
+/* (src/general_primitive_integral.F90:9-194) */
+static double general_primitive_integral(const double *P_new, const double *P_center, double fact_p,
+                                         double p, double p_inv, const int *iorder_p,
+                                         const double *Q_new, const double *Q_center, double fact_q,
+                                         double q, double q_inv, const int *iorder_q) {
+  double Ix_pol[MAXD], Iy_pol[MAXD], Iz_pol[MAXD], dx[MAXD], d_poly[MAXD], d1[MAXD];
+  int n_Ix, n_Iy, n_Iz, nx;
+  double pq = p_inv * 0.5 * q_inv;
+  double pq_inv = 0.5 / (p + q);
+  double p10_1 = q * pq;
+  double p01_1 = p * pq;
+  double pq_inv_2 = pq_inv + pq_inv;
+  double p10_2 = pq_inv_2 * p10_1 * q;
+  double p01_2 = pq_inv_2 * p01_1 * p;
+  int iorder;
+
+  /* Ix: note the x-axis skips |P| < thresh, y and z process |P| > thresh */
+  iorder = iorder_p[0] + iorder_q[0] + iorder_p[0] + iorder_q[0];
+  for (int ix = 0; ix <= iorder; ix++) Ix_pol[ix] = 0.0;
+  n_Ix = 0;
+  for (int ix = 0; ix <= iorder_p[0]; ix++) {
+    if (fabs(P_new[ix]) < THRESH) continue;
+    double a = P_new[ix];
+    for (int jx = 0; jx <= iorder_q[0]; jx++) {
+      double d = a * Q_new[jx];
+      if (fabs(d) < THRESH) continue;
+      give_polynom_mult_center_x(P_center[0], Q_center[0], ix, jx, p, q, iorder, pq_inv, pq_inv_2,
+                                 p10_1, p01_1, p10_2, p01_2, dx, &nx);
+      add_poly_multiply(dx, nx, d, Ix_pol, &n_Ix);
+    }
+  }
+  if (n_Ix == -1) return 0.0;
+
+  iorder = iorder_p[1] + iorder_q[1] + iorder_p[1] + iorder_q[1];
+  for (int ix = 0; ix <= iorder; ix++) Iy_pol[ix] = 0.0;
+  n_Iy = 0;
+  for (int iy = 0; iy <= iorder_p[1]; iy++) {
+    if (fabs(P_new[MAXD + iy]) > THRESH) {
+      double b = P_new[MAXD + iy];
+      for (int jy = 0; jy <= iorder_q[1]; jy++) {
+        double e = b * Q_new[MAXD + jy];
+        if (fabs(e) < THRESH) continue;
+        give_polynom_mult_center_x(P_center[1], Q_center[1], iy, jy, p, q, iorder, pq_inv,
+                                   pq_inv_2, p10_1, p01_1, p10_2, p01_2, dx, &nx);
+        add_poly_multiply(dx, nx, e, Iy_pol, &n_Iy);
+      }
+    }
+  }
+  if (n_Iy == -1) return 0.0;
+
+  iorder = iorder_p[2] + iorder_q[2] + iorder_p[2] + iorder_q[2];
+  for (int ix = 0; ix <= iorder; ix++) Iz_pol[ix] = 0.0;
+  n_Iz = 0;
+  for (int iz = 0; iz <= iorder_p[2]; iz++) {
+    if (fabs(P_new[2 * MAXD + iz]) > THRESH) {
+      double c = P_new[2 * MAXD + iz];
+      for (int jz = 0; jz <= iorder_q[2]; jz++) {
+        double f = c * Q_new[2 * MAXD + jz];
+        if (fabs(f) < THRESH) continue;
+        give_polynom_mult_center_x(P_center[2], Q_center[2], iz, jz, p, q, iorder, pq_inv,
+                                   pq_inv_2, p10_1, p01_1, p10_2, p01_2, dx, &nx);
+        add_poly_multiply(dx, nx, f, Iz_pol, &n_Iz);
+      }
+    }
+  }
+  if (n_Iz == -1) return 0.0;
+
+  double rho = p * q * pq_inv_2;
+  double dist = (P_center[0] - Q_center[0]) * (P_center[0] - Q_center[0]) +
+                (P_center[1] - Q_center[1]) * (P_center[1] - Q_center[1]) +
+                (P_center[2] - Q_center[2]) * (P_center[2] - Q_center[2]);
+  double cst = dist * rho;
+
+  int n_pt_tmp = n_Ix + n_Iy;
+  for (int i = 0; i <= n_pt_tmp; i++) d_poly[i] = 0.0;
+  multiply_poly(Ix_pol, n_Ix, Iy_pol, n_Iy, d_poly, &n_pt_tmp);
+  if (n_pt_tmp == -1) return 0.0;
+  int n_pt_out = n_pt_tmp + n_Iz;
+  for (int i = 0; i <= n_pt_out; i++) d1[i] = 0.0;
+  multiply_poly(d_poly, n_pt_tmp, Iz_pol, n_Iz, d1, &n_pt_out);
+
+  double accu = 0.0;
+  accu = accu + orc_rint_sum(n_pt_out, cst, d1);
+  return fact_p * fact_q * accu * PI_5_2 * p_inv * q_inv / sqrt(p + q);
+}
+
+/* (src/bielec_integral.F90:1-55) */
+double orc_bielec_integral(double alpha, double beta, double delta, double gama, const double *A,
+                           const double *B, const double *C, const double *D, const int *pA,
+                           const int *pB, const int *pC, const int *pD) {
+  init_tables();
+  double P_new[3 * MAXD], Q_new[3 * MAXD], P_center[3], Q_center[3], pp, qq, fact_p, fact_q;
+  int iorder_p[3], iorder_q[3];
+  give_explicit_poly_and_gaussian(P_new, P_center, &pp, &fact_p, iorder_p, alpha, beta, pA, pB, A, B);
+  double p_inv = 1.0 / pp;
+  give_explicit_poly_and_gaussian(Q_new, Q_center, &qq, &fact_q, iorder_q, delta, gama, pC, pD, C, D);
+  double q_inv = 1.0 / qq;
+  return general_primitive_integral(P_new, P_center, fact_p, pp, p_inv, iorder_p, Q_new, Q_center,
+                                    fact_q, qq, q_inv, iorder_q);
+}
+
+/* ------------------------------------------------------------------ */
+/* contracted ERI of the fits                                          */
+/* ------------------------------------------------------------------ */
+#define CG(b, m, i, t) ((b)->c_gauss[(m) + (int64_t)(b)->ld * ((i) + (int64_t)(b)->n * (t))])
+#define GG(b, m, i) ((b)->g_gauss[(m) + (int64_t)(b)->ld * (i)])
+
+/* cartesian components of one fitted function (src/gauss_ijkl.F90:68-123) */
+static int components(const orc_basis *b, int io, int n_c[4][3], int *coef_t) {
+  const int *np = b->npower + 3 * io;
+  int it = b->i_type[io];
+  if (it == 1) {
+    for (int l = 0; l < 3; l++) n_c[0][l] = np[l];
+    coef_t[0] = 0;
+    return 1;
+  }
+  if (it == 2) {
+    for (int ii = 0; ii < 3; ii++) {
+      for (int l = 0; l < 3; l++) n_c[ii][l] = np[l] + (l == ii ? 2 : 0);
+      coef_t[ii] = 1;
+    }
+    return 3;
+  }
+  /* i_type 3: r^0 and r^2 parts */
+  for (int ii = 0; ii < 4; ii++) {
+    for (int l = 0; l < 3; l++) n_c[ii][l] = np[l] + (l == ii - 1 ? 2 : 0);
+    coef_t[ii] = ii == 0 ? 0 : 1;
+  }
+  return 4;
+}
+
+/* 0: sequential FP64 accumulation as the reference (src/gauss_ijkl.F90:125-152);
+ * 1: same terms accumulated in long double (the exactly-summed value the parity tests use,
+ *    since the reference's own sequential sum over ~1e7 terms carries ~1e-12 rounding). */
+static int g_sum_mode = 0;
+void orc_set_sum_mode(int mode) { g_sum_mode = mode; }
+
+double orc_gauss_ijkl(const orc_basis *b, int i, int k, int j, int l) {
+  init_tables();
+  int orb[4] = {i, k, j, l};
+  int nc[4], n_c[4][4][3], ct[4][4];
+  for (int kk = 0; kk < 4; kk++) nc[kk] = components(b, orb[kk], n_c[kk], ct[kk]);
+  const double *A = b->center + 3 * i, *B = b->center + 3 * k, *C = b->center + 3 * j,
+               *D = b->center + 3 * l;
+  double rint = 0.0;
+  long double rint_ext = 0.0L;
+  for (int i1 = 0; i1 < b->n_gauss[i]; i1++)
+    for (int i2 = 0; i2 < b->n_gauss[k]; i2++)
+      for (int i3 = 0; i3 < b->n_gauss[j]; i3++)
+        for (int i4 = 0; i4 < b->n_gauss[l]; i4++)
+          for (int ii1 = 0; ii1 < nc[0]; ii1++)
+            for (int ii2 = 0; ii2 < nc[1]; ii2++)
+              for (int ii3 = 0; ii3 < nc[2]; ii3++)
+                for (int ii4 = 0; ii4 < nc[3]; ii4++) {
+                  double d1 = CG(b, i1, i, ct[0][ii1]);
+                  double d2 = CG(b, i2, k, ct[1][ii2]);
+                  double d3 = CG(b, i3, j, ct[2][ii3]);
+                  double d4 = CG(b, i4, l, ct[3][ii4]);
+                  double term = d1 * d2 * d3 * d4 *
+                                orc_bielec_integral(GG(b, i1, i), GG(b, i2, k), GG(b, i3, j),
+                                                    GG(b, i4, l), A, B, C, D, n_c[0][ii1],
+                                                    n_c[1][ii2], n_c[2][ii3], n_c[3][ii4]);
+                  rint = rint + term;
+                  rint_ext += (long double)term;
+                }
+  return g_sum_mode ? (double)rint_ext : rint;
+}
+
+static int nc_of(const orc_basis *b, int io) {
+  int t = b->i_type[io];
+  return t == 1 ? 1 : (t == 2 ? 3 : 4);
+}
+
+double orc_count_primitive_quartets(const orc_basis *b, int64_t nint, const int32_t *is,
+                                    const int32_t *js, const int32_t *ks, const int32_t *ls) {
+  double tot = 0.0;
+  for (int64_t q = 0; q < nint; q++) {
+    int o[4] = {is[q] - 1, ks[q] - 1, js[q] - 1, ls[q] - 1};
+    double c = 1.0;
+    for (int t = 0; t < 4; t++) c *= (double)(b->n_gauss[o[t]] * nc_of(b, o[t]));
+    tot += c;
+  }
+  return tot;
+}
+
+void orc_precond(const orc_basis *b, double *precond, int nthreads) {
+  int n = b->n;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+  for (int k = 0; k < n; k++)
+    for (int i = 0; i < n; i++) precond[i + n * k] = orc_gauss_ijkl(b, i, k, i, k);
+}
+
+int64_t orc_gauss_eri(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                      const int32_t *ks, const int32_t *ls, const double *precond, double *out,
+                      int nthreads) {
+  const double seuil = 1.e-15;
+  int n = b->n;
+  int64_t nzero = 0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : nzero)
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    double pik = precond[i + n * k], pjl = precond[j + n * l];
+    if (fabs(pik * pjl) < seuil * seuil) nzero++;
+    if (i == j && k == l)
+      out[q] = pik;
+    else if (fabs(pik * pjl) >= seuil * seuil)
+      out[q] = orc_gauss_ijkl(b, i, k, j, l);
+    else
+      out[q] = 0.0;
+  }
+  return nzero;
+}
+
+/* ------------------------------------------------------------------ */
+/* walker transform (src/dierfc.F90:3-68)                              */
+/* ------------------------------------------------------------------ */
+double orc_dierfc(double y) {
+  const double qa = 9.16461398268964e-01, qb = 2.31729200323405e-01, qc = 4.88826640273108e-01,
+               qd = 1.24610454613712e-01, q0 = 4.99999303439796e-01, q1 = 1.16065025341614e-01,
+               q2 = 1.50689047360223e-01, q3 = 2.69999308670029e-01, q4 = -7.28846765585675e-02;
+  const double pa = 3.97886080735226000e+00, pb = 1.20782237635245222e-01,
+               p0 = 2.44044510593190935e-01, p1 = 4.34397492331430115e-01,
+               p2 = 6.86265948274097816e-01, p3 = 9.56464974744799006e-01,
+               p4 = 1.16374581931560831e+00, p5 = 1.21448730779995237e+00,
+               p6 = 1.05375024970847138e+00, p7 = 7.13657635868730364e-01,
+               p8 = 3.16847638520135944e-01, p9 = 1.47297938331485121e-02,
+               p10 = -1.05872177941595488e-01, p11 = -7.43424357241784861e-02,
+               p12 = 2.20995927012179067e-03, p13 = 3.46494207789099922e-02,
+               p14 = 1.42961988697898018e-02, p15 = -1.18598117047771104e-02,
+               p16 = -1.12749169332504870e-02, p17 = 3.39721910367775861e-03,
+               p18 = 6.85649426074558612e-03, p19 = -7.71708358954120939e-04,
+               p20 = -3.51287146129100025e-03, p21 = 1.05739299623423047e-04,
+               p22 = 1.12648096188977922e-03;
+  double z = y, w, u, s, t, x;
+  if (y > 1.0) z = 2.0 - y;
+  w = qa - log(z);
+  u = sqrt(w);
+  s = (qc + log(u)) / w;
+  t = 1.0 / (u + qb);
+  x = u * (1 - s * (0.5 + s * qd)) - ((((q4 * t + q3) * t + q2) * t + q1) * t + q0) * t;
+  t = pa / (pa + x);
+  u = t - 0.5;
+  s = (((((((((p22 * u + p21) * u + p20) * u + p19) * u + p18) * u + p17) * u + p16) * u + p15) *
+            u + p14) * u + p13) * u + p12;
+  s = ((((((((((((s * u + p11) * u + p10) * u + p9) * u + p8) * u + p7) * u + p6) * u + p5) * u +
+             p4) * u + p3) * u + p2) * u + p1) * u + p0) * t -
+      z * exp(x * x - pb);
+  x = x + s * (1.0 + x * s);
+  if (y > 1.0) x = -x;
+  return x;
+}
+
+/* ------------------------------------------------------------------ */
+/* pair densities (src/compute_densities.F90:1-95, u_orb.F90, u_gauss.F90) */
+/* ------------------------------------------------------------------ */
+static double u_orb(const orc_basis *b, int i, double r) {
+  /* c_contract = 1 (src/read_basis.F90:35), single contraction (src/u_orb.F90:8-27) */
+  double g = b->g_slater[i];
+  switch (b->n_sto[i]) {
+    case 0: return 1.0 * exp(-g * r);
+    case 1: return 1.0 * r * exp(-g * r);
+    case 2: { double r2 = r * r; return 1.0 * r2 * exp(-g * r); }
+    case 3: { double r2 = r * r; return 1.0 * r2 * r * exp(-g * r); }
+    case 4: { double r2 = r * r; return 1.0 * r2 * r2 * exp(-g * r); }
+    default: return 1.0 * pow(r, b->n_sto[i]) * exp(-g * r);
+  }
+}
+
+static double u_gauss(const orc_basis *b, int i, double r) {
+  double r2 = r * r, u = 0.0;
+  for (int m = 0; m < b->n_gauss[i]; m++)
+    u = u + (CG(b, m, i, 0) + CG(b, m, i, 1) * r2) * exp(-GG(b, m, i) * r2);
+  return u;
+}
+
+/* one electron's pair densities at point u (src/compute_densities.F90:17-53) */
+static void pair_density_at(const orc_basis *b, int i, int k, const double *u, double *rS,
+                            double *rG) {
+  const double *ci = b->center + 3 * i, *ck = b->center + 3 * k;
+  const int *pi = b->npower + 3 * i, *pk = b->npower + 3 * k;
+  double dx = u[0] - ci[0], dy = u[1] - ci[1], dz = u[2] - ci[2];
+  double poly_i = 1.0;
+  for (int t = 0; t < pi[0]; t++) poly_i = poly_i * dx;
+  for (int t = 0; t < pi[1]; t++) poly_i = poly_i * dy;
+  for (int t = 0; t < pi[2]; t++) poly_i = poly_i * dz;
+  double r_i = sqrt(dx * dx + dy * dy + dz * dz);
+  dx = u[0] - ck[0]; dy = u[1] - ck[1]; dz = u[2] - ck[2];
+  double poly_k = 1.0;
+  for (int t = 0; t < pk[0]; t++) poly_k = poly_k * dx;
+  for (int t = 0; t < pk[1]; t++) poly_k = poly_k * dy;
+  for (int t = 0; t < pk[2]; t++) poly_k = poly_k * dz;
+  double r_k = sqrt(dx * dx + dy * dy + dz * dz);
+  double poly_ik = poly_i * poly_k;
+  *rS = poly_ik * u_orb(b, i, r_i) * u_orb(b, k, r_k);
+  *rG = poly_ik * u_gauss(b, i, r_i) * u_gauss(b, k, r_k);
+}
+
+void orc_pair_densities(const orc_basis *b, int npairs, const int *ip, const int *kp, int64_t S,
+                        const double *u, double *rhoS, double *rhoG) {
+#pragma omp parallel for schedule(static)
+  for (int p = 0; p < npairs; p++)
+    for (int64_t s = 0; s < S; s++)
+      pair_density_at(b, ip[p], kp[p], u + 3 * s, rhoS + (int64_t)p * S + s, rhoG + (int64_t)p * S + s);
+}
+
+/* ------------------------------------------------------------------ */
+/* faithful ZV-MC (src/two_e_slater.F90:339-496)                       */
+/* ------------------------------------------------------------------ */
+#define NW 40         /* walkers per chunk, src/common_data.F90:4 */
+#define SUPER (NW * 64) /* walkers whose densities are held at once */
+
+int orc_zvmc_faithful(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                      const int32_t *ks, const int32_t *ls, double a_zv, const double *r1,
+                      const double *r2, int nblocks, int64_t npts, int mode, double *mean,
+                      double *err, double *xb, int nthreads) {
+  init_tables();
+  if (npts % NW != 0) return -1; /* src/two_e_slater.F90:148 */
+  int n = b->n;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  /* pair table: pair index for (i,k), i >= k, that is used (src/two_e_slater.F90:373-382) */
+  int *pidx = (int *)malloc(sizeof(int) * n * n);
+  for (int t = 0; t < n * n; t++) pidx[t] = -1;
+  int np = 0;
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    if (pidx[i + n * k] < 0) pidx[i + n * k] = np++;
+    if (pidx[j + n * l] < 0) pidx[j + n * l] = np++;
+  }
+  int *pi_ = (int *)malloc(sizeof(int) * np), *pk_ = (int *)malloc(sizeof(int) * np);
+  for (int k = 0; k < n; k++)
+    for (int i = 0; i < n; i++)
+      if (pidx[i + n * k] >= 0) { pi_[pidx[i + n * k]] = i; pk_[pidx[i + n * k]] = k; }
+  /* G_center and ZV factors (src/two_e_slater.F90:339-348, :406) */
+  double *G = (double *)malloc(sizeof(double) * 3 * np);
+  double *fzv = (double *)malloc(sizeof(double) * np);  /* 0.5 a / (g_i+g_k) */
+  double *fjac = (double *)malloc(sizeof(double) * np); /* a / (g_i+g_k) */
+  for (int p = 0; p < np; p++) {
+    int i = pi_[p], k = pk_[p];
+    double gi = b->g_slater[i], gk = b->g_slater[k];
+    for (int l = 0; l < 3; l++)
+      G[3 * p + l] = (gi * b->center[l + 3 * i] + gk * b->center[l + 3 * k]) / (gi + gk);
+    fzv[p] = 0.5 * a_zv / (gi + gk);
+    fjac[p] = a_zv / (gi + gk);
+  }
+  /* per super-chunk buffers: [p][s] */
+  size_t ps = (size_t)np * SUPER;
+  double *ut1 = (double *)malloc(sizeof(double) * 3 * ps), *ut2 = (double *)malloc(sizeof(double) * 3 * ps);
+  double *rh1 = (double *)malloc(sizeof(double) * ps), *rh2 = (double *)malloc(sizeof(double) * ps);
+  double *rg1 = (double *)malloc(sizeof(double) * ps), *rg2 = (double *)malloc(sizeof(double) * ps);
+  double *j1 = (double *)malloc(sizeof(double) * ps), *j2 = (double *)malloc(sizeof(double) * ps);
+  double *pi0 = (double *)malloc(sizeof(double) * SUPER);
+  double *eS = (double *)malloc(sizeof(double) * nint), *eG = (double *)malloc(sizeof(double) * nint);
+  double *acc = (double *)calloc(nint, sizeof(double)), *acc2 = (double *)calloc(nint, sizeof(double));
+  const double fpi0 = 1.0 / ((2.0 * M_PI) * (2.0 * M_PI) * (2.0 * M_PI));
+
+  for (int blk = 0; blk < nblocks; blk++) {
+    for (int64_t q = 0; q < nint; q++) eS[q] = eG[q] = 0.0;
+    for (int64_t s0 = 0; s0 < npts; s0 += SUPER) {
+      int ns = (int)((npts - s0) < SUPER ? (npts - s0) : SUPER);
+      const double *R1 = r1 + 3 * ((int64_t)blk * npts + s0);
+      const double *R2 = r2 + 3 * ((int64_t)blk * npts + s0);
+      /* pi_0 (src/compute_jacobian_and_pi0.F90:12-18) */
+      for (int s = 0; s < ns; s++) {
+        double m1 = R1[3 * s] * R1[3 * s] + R1[3 * s + 1] * R1[3 * s + 1] + R1[3 * s + 2] * R1[3 * s + 2];
+        double m2 = R2[3 * s] * R2[3 * s] + R2[3 * s + 1] * R2[3 * s + 1] + R2[3 * s + 2] * R2[3 * s + 2];
+        pi0[s] = exp(-0.5 * (m1 + m2)) * fpi0;
+      }
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int p = 0; p < np; p++) {
+        int i = pi_[p], k = pk_[p];
+        for (int s = 0; s < ns; s++) {
+          const double *a1 = R1 + 3 * s, *a2 = R2 + 3 * s;
+          double r1m = sqrt(a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2]);
+          double r2m = sqrt(a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2]);
+          double u1[3], u2[3];
+          for (int l = 0; l < 3; l++) {
+            u1[l] = fzv[p] * a1[l] * r1m + G[3 * p + l]; /* src/two_e_slater.F90:410 */
+            u2[l] = fzv[p] * a2[l] * r2m + G[3 * p + l];
+            ut1[(size_t)p * 3 * SUPER + 3 * s + l] = u1[l];
+            ut2[(size_t)p * 3 * SUPER + 3 * s + l] = u2[l];
+          }
+          pair_density_at(b, i, k, u1, &rh1[(size_t)p * SUPER + s], &rg1[(size_t)p * SUPER + s]);
+          pair_density_at(b, i, k, u2, &rh2[(size_t)p * SUPER + s], &rg2[(size_t)p * SUPER + s]);
+          /* src/compute_jacobian_and_pi0.F90:22-30 */
+          double f1 = fjac[p] * r1m, f2 = fjac[p] * r2m;
+          j1[(size_t)p * SUPER + s] = 0.25 * fabs(f1 * f1 * f1);
+          j2[(size_t)p * SUPER + s] = 0.25 * fabs(f2 * f2 * f2);
+        }
+      }
+      /* accumulation (src/two_e_slater.F90:424-453), chunks of NW walkers */
+#pragma omp parallel for schedule(static)
+      for (int64_t q = 0; q < nint; q++) {
+        int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+        int pik = pidx[i + n * k], pjl = pidx[j + n * l];
+        const double *U1 = ut1 + (size_t)pik * 3 * SUPER, *U2 = ut2 + (size_t)pjl * 3 * SUPER;
+        const double *RS1 = rh1 + (size_t)pik * SUPER, *RS2 = rh2 + (size_t)pjl * SUPER;
+        const double *RG1 = rg1 + (size_t)pik * SUPER, *RG2 = rg2 + (size_t)pjl * SUPER;
+        const double *J1 = j1 + (size_t)pik * SUPER, *J2 = j2 + (size_t)pjl * SUPER;
+        double es = eS[q], eg = eG[q];
+        for (int c0 = 0; c0 < ns; c0 += NW) {
+          double sw = 0.0, swg = 0.0;
+          for (int kw = c0; kw < c0 + NW; kw++) {
+            double dx0 = U1[3 * kw] - U2[3 * kw];
+            double dx1 = U1[3 * kw + 1] - U2[3 * kw + 1];
+            double dx2 = U1[3 * kw + 2] - U2[3 * kw + 2];
+            double r12_2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+            double rjacob = J1[kw] * J2[kw];
+            double factor, r12_inv;
+            if (mode == 0) {
+              factor = (double)((float)rjacob / (float)pi0[kw]);
+              r12_inv = (double)(1.0f / sqrtf((float)r12_2));
+            } else {
+              factor = rjacob / pi0[kw];
+              r12_inv = 1.0 / sqrt(r12_2);
+            }
+            double weight = factor * RS1[kw] * RS2[kw];
+            double weight_G = factor * RG1[kw] * RG2[kw];
+            sw = sw + weight * r12_inv;
+            swg = swg + weight_G * r12_inv;
+          }
+          es = es + sw;
+          eg = eg + swg;
+        }
+        eS[q] = es;
+        eG[q] = eg;
+      }
+    }
+    /* block moments (src/two_e_slater.F90:463-481) */
+    double factor = 1.0 / (double)npts;
+    for (int64_t q = 0; q < nint; q++) {
+      double x = eS[q] * factor - eG[q] * factor;
+      if (xb) xb[(int64_t)blk * nint + q] = x;
+      acc[q] = acc[q] + x;
+      acc2[q] = acc2[q] + x * x;
+    }
+  }
+  /* src/two_e_slater.F90:488-492 */
+  for (int64_t q = 0; q < nint; q++) {
+    double m = acc[q] / nblocks, m2 = acc2[q] / nblocks;
+    mean[q] = m;
+    err[q] = sqrt(fabs(m2 - m * m)) / sqrt((double)nblocks);
+  }
+  free(pidx); free(pi_); free(pk_); free(G); free(fzv); free(fjac);
+  free(ut1); free(ut2); free(rh1); free(rh2); free(rg1); free(rg2); free(j1); free(j2);
+  free(pi0); free(eS); free(eG); free(acc); free(acc2);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* shared-walker estimator in FP64                                     */
+/* ------------------------------------------------------------------ */
+int orc_zvmc_shared(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                    const int32_t *ks, const int32_t *ls, const double *u1, const double *u2,
+                    const double *w, int nblocks, int64_t npts, int symmetrize, double *mean,
+                    double *err, double *xb, int nthreads) {
+  init_tables();
+  int n = b->n;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  int *pidx = (int *)malloc(sizeof(int) * n * n);
+  for (int t = 0; t < n * n; t++) pidx[t] = -1;
+  int np = 0;
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    if (pidx[i + n * k] < 0) pidx[i + n * k] = np++;
+    if (pidx[j + n * l] < 0) pidx[j + n * l] = np++;
+  }
+  int *pi_ = (int *)malloc(sizeof(int) * np), *pk_ = (int *)malloc(sizeof(int) * np);
+  for (int k = 0; k < n; k++)
+    for (int i = 0; i < n; i++)
+      if (pidx[i + n * k] >= 0) { pi_[pidx[i + n * k]] = i; pk_[pidx[i + n * k]] = k; }
+  const int CH = 4096;
+  size_t ps = (size_t)np * CH;
+  double *s1 = (double *)malloc(sizeof(double) * ps), *g1 = (double *)malloc(sizeof(double) * ps);
+  double *s2 = (double *)malloc(sizeof(double) * ps), *g2 = (double *)malloc(sizeof(double) * ps);
+  double *e = (double *)malloc(sizeof(double) * nint);
+  double *acc = (double *)calloc(nint, sizeof(double)), *acc2 = (double *)calloc(nint, sizeof(double));
+  for (int blk = 0; blk < nblocks; blk++) {
+    for (int64_t q = 0; q < nint; q++) e[q] = 0.0;
+    for (int64_t s0 = 0; s0 < npts; s0 += CH) {
+      int ns = (int)((npts - s0) < CH ? (npts - s0) : CH);
+      int64_t base = (int64_t)blk * npts + s0;
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int p = 0; p < np; p++)
+        for (int s = 0; s < ns; s++) {
+          pair_density_at(b, pi_[p], pk_[p], u1 + 3 * (base + s), &s1[(size_t)p * CH + s], &g1[(size_t)p * CH + s]);
+          pair_density_at(b, pi_[p], pk_[p], u2 + 3 * (base + s), &s2[(size_t)p * CH + s], &g2[(size_t)p * CH + s]);
+        }
+#pragma omp parallel for schedule(static)
+      for (int64_t q = 0; q < nint; q++) {
+        int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+        size_t a = (size_t)pidx[i + n * k] * CH, c = (size_t)pidx[j + n * l] * CH;
+        double t = 0.0;
+        for (int s = 0; s < ns; s++) {
+          double x = (s1[a + s] * s2[c + s] - g1[a + s] * g2[c + s]);
+          if (symmetrize) x = 0.5 * (x + (s1[c + s] * s2[a + s] - g1[c + s] * g2[a + s]));
+          t += x * w[base + s];
+        }
+        e[q] += t;
+      }
+    }
+    for (int64_t q = 0; q < nint; q++) {
+      double x = e[q] / (double)npts;
+      if (xb) xb[(int64_t)blk * nint + q] = x;
+      acc[q] += x;
+      acc2[q] += x * x;
+    }
+  }
+  for (int64_t q = 0; q < nint; q++) {
+    double m = acc[q] / nblocks, m2 = acc2[q] / nblocks;
+    mean[q] = m;
+    err[q] = nblocks > 1 ? sqrt(fabs(m2 - m * m) / (double)(nblocks - 1)) : 0.0;
+  }
+  free(pidx); free(pi_); free(pk_); free(s1); free(g1); free(s2); free(g2); free(e); free(acc); free(acc2);
+  return 0;
+}

@@ -1,0 +1,469 @@
+// shared.cu -- shared-walker estimator: mixture sampler, FP32 orbital densities, split-BF16
+// operand producer, block statistics, and the host loop around the tcgen05 GEMM.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mc.cuh"
+#include "philox.cuh"
+#include "shared.cuh"
+#include "ss_common.cuh"
+#include "ss_context.cuh"
+
+namespace ss {
+
+struct MixDev {
+  int m;
+  const double* G;      // [3m]
+  const double* c;      // [m]
+  const double* cdf;    // [m], cdf[m-1] == 1
+  const float* Gf;      // [3m]
+  const float* inv2c;   // 1/(2c)
+  const float* norm;    // w_c / ((2 pi)^{3/2} 2 c^{3/2})
+};
+
+__device__ __forceinline__ int pick_component(const MixDev& M, double u) {
+  int lo = 0, hi = M.m - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (u <= M.cdf[mid]) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+// mixture density pi(u) = sum_c norm_c exp(-|u-G_c|/(2c)) |u-G_c|^{-3/2}
+__device__ __forceinline__ float mixture_density(const MixDev& M, const double (&u)[3]) {
+  float tot = 0.f;
+  for (int c = 0; c < M.m; c++) {
+    float dx = (float)(u[0] - M.G[3 * c]), dy = (float)(u[1] - M.G[3 * c + 1]), dz = (float)(u[2] - M.G[3 * c + 2]);
+    float rho = sqrtf(dx * dx + dy * dy + dz * dz);
+    float ir = rsqrtf(rho);
+    tot += M.norm[c] * __expf(-rho * M.inv2c[c]) * (ir * ir * ir);
+  }
+  return tot;
+}
+
+__device__ __forceinline__ void zv_point(const MixDev& M, int c, const double (&n)[3], double (&u)[3]) {
+  const double r = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double cc = M.c[c];
+#pragma unroll
+  for (int l = 0; l < 3; l++) u[l] = cc * n[l] * r + M.G[3 * c + l];
+}
+
+// samples of one block: u1, u2 [3S] (double), w [S]
+__global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, MixDev M, double* __restrict__ u1,
+                                     double* __restrict__ u2, double* __restrict__ w) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int64_t g = first + s;
+  double uu[8];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    uint32_t cnt[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), (uint32_t)j, STREAM_SHARED};
+    philox4x32_10(cnt, (uint32_t)seed, (uint32_t)(seed >> 32));
+    uu[2 * j] = u01_open(cnt[0], cnt[1]);
+    uu[2 * j + 1] = u01_open(cnt[2], cnt[3]);
+  }
+  const int c1 = pick_component(M, uu[0]);
+  const int c2 = pick_component(M, uu[4]);
+  double n1[3] = {normcdfinv(uu[1]), normcdfinv(uu[2]), normcdfinv(uu[3])};
+  double n2[3] = {normcdfinv(uu[5]), normcdfinv(uu[6]), normcdfinv(uu[7])};
+  double a[3], b[3];
+  zv_point(M, c1, n1, a);
+  zv_point(M, c2, n2, b);
+  const float p1 = mixture_density(M, a), p2 = mixture_density(M, b);
+  const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+  const float r12 = (float)sqrt(dx * dx + dy * dy + dz * dz);
+  const float ww = 1.0f / (r12 * p1 * p2);
+  u1[3 * s] = a[0]; u1[3 * s + 1] = a[1]; u1[3 * s + 2] = a[2];
+  u2[3 * s] = b[0]; u2[3 * s + 1] = b[1]; u2[3 * s + 2] = b[2];
+  w[s] = isfinite(ww) ? (double)ww : 0.0;
+}
+
+// Orbital values at the samples (the factors of src/compute_densities.F90:51-53):
+// phiS_i = poly_i u_orb_i, phiG_i = poly_i u_gauss_i and the fit residual
+// delta_i = poly_i (u_orb_i - u_gauss_i).  With 20-Gaussian fits delta/phi is 1e-5..1e-8, so the
+// residual is formed in FP64 (a difference of two FP32 values would be rounding noise); Gaussian
+// terms whose exponent exceeds the most diffuse term's by more than 60 (relative size < 1e-26
+// times a coefficient ratio) are skipped.  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
+__global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, const double* __restrict__ u1,
+                                         const double* __restrict__ u2, float* __restrict__ out) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (s >= S) return;
+  const double* A = B.center + 3 * i;
+  const int px = B.npower[3 * i], py = B.npower[3 * i + 1], pz = B.npower[3 * i + 2];
+  const int nsto = B.n_sto[i];
+  const double zeta = B.g_slater[i];
+  const int ng = B.n_gauss[i];
+  const double* c1 = B.c_gauss + (int64_t)B.ld * i;
+  const double* c2 = B.c_gauss + (int64_t)B.ld * (i + (int64_t)B.n);
+  const double* gg = B.g_gauss + (int64_t)B.ld * i;
+  float gmin = 3.0e38f;
+  for (int m = 0; m < ng; m++) gmin = fminf(gmin, (float)gg[m]);
+  const int64_t plane = (int64_t)B.n * ld;
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const double* u = e == 0 ? u1 : u2;
+    const double dx = u[3 * s] - A[0], dy = u[3 * s + 1] - A[1], dz = u[3 * s + 2] - A[2];
+    double poly = 1.0;
+    for (int t = 0; t < px; t++) poly *= dx;
+    for (int t = 0; t < py; t++) poly *= dy;
+    for (int t = 0; t < pz; t++) poly *= dz;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double r = sqrt(r2);
+    double uo = exp(-zeta * r);
+    for (int t = 0; t < nsto; t++) uo *= r;
+    const float r2f = (float)r2;
+    const float ycut = gmin * r2f + 60.0f;
+    double ug = 0.0;
+    for (int m = 0; m < ng; m++) {
+      if ((float)gg[m] * r2f > ycut) continue;
+      ug += (c1[m] + c2[m] * r2) * exp(-gg[m] * r2);
+    }
+    const int64_t o = (int64_t)i * ld + s;
+    out[(3 * e) * plane + o] = (float)(poly * uo);
+    out[(3 * e + 1) * plane + o] = (float)(poly * ug);
+    out[(3 * e + 2) * plane + o] = (float)(poly * (uo - ug));
+  }
+}
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// operands of one sub-chunk: A = [Delta1 | rhoG1], B = [rhoS2 w | Delta2 w], rows = pairs,
+// K = 2*Kh (Kh >= S, padded samples are zero); hi/lo BF16 split.
+__global__ void shared_operand_kernel(int64_t S, int64_t Kh, int64_t ld, int n, const int* __restrict__ pi,
+                                      const int* __restrict__ pk, const float* __restrict__ F,
+                                      const double* __restrict__ w, __nv_bfloat16* __restrict__ Ahi,
+                                      __nv_bfloat16* __restrict__ Alo, __nv_bfloat16* __restrict__ Bhi,
+                                      __nv_bfloat16* __restrict__ Blo) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (s >= Kh) return;
+  float d1 = 0.f, g1 = 0.f, s2w = 0.f, d2w = 0.f;
+  if (s < S) {
+    const int i = pi[p], k = pk[p];
+    const int64_t plane = (int64_t)n * ld;
+    const float* F1S = F;
+    const float* F1G = F + plane;
+    const float* F1D = F + 2 * plane;
+    const float* F2S = F + 3 * plane;
+    const float* F2G = F + 4 * plane;
+    const float* F2D = F + 5 * plane;
+    const int64_t oi = (int64_t)i * ld + s, ok = (int64_t)k * ld + s;
+    const float ww = (float)w[s];
+    // rhoS - rhoG = phiS_i delta_k + delta_i phiG_k (exact identity, no cancellation)
+    d1 = fmaf(F1S[oi], F1D[ok], F1D[oi] * F1G[ok]);
+    g1 = F1G[oi] * F1G[ok];
+    s2w = (F2S[oi] * F2S[ok]) * ww;
+    d2w = fmaf(F2S[oi], F2D[ok], F2D[oi] * F2G[ok]) * ww;
+  }
+  const int64_t K = 2 * Kh;
+  const int64_t r = (int64_t)p * K;
+  __nv_bfloat16 h, l;
+  split_bf16(d1, h, l); Ahi[r + s] = h; Alo[r + s] = l;
+  split_bf16(g1, h, l); Ahi[r + Kh + s] = h; Alo[r + Kh + s] = l;
+  split_bf16(s2w, h, l); Bhi[r + s] = h; Blo[r + s] = l;
+  split_bf16(d2w, h, l); Bhi[r + Kh + s] = h; Blo[r + Kh + s] = l;
+}
+
+// Cblk[P][P] (double) += sum over K slices of the fp32 partial products
+__global__ void shared_accumulate_block(int P, int ksplit, const float* __restrict__ Cp, double* __restrict__ Cblk) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t PP = (int64_t)P * P;
+  if (e >= PP) return;
+  double v = 0.0;
+  for (int t = 0; t < ksplit; t++) v += (double)Cp[t * PP + e];
+  Cblk[e] += v;
+}
+
+// per-quartet block value x = (C[ik][jl] + C[jl][ik]) / (2 npts)  (electron-swap symmetrised)
+__global__ void shared_block_stats(int64_t nint, int P, int64_t npts, const int* __restrict__ p1,
+                                   const int* __restrict__ p2, double* __restrict__ Cblk,
+                                   double* __restrict__ acc, double* __restrict__ acc2) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int64_t a = (int64_t)p1[q] * P + p2[q], b = (int64_t)p2[q] * P + p1[q];
+  const double x = 0.5 * (Cblk[a] + Cblk[b]) / (double)npts;
+  acc[q] += x;
+  acc2[q] += x * x;
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------
+#define TRY(x)           \
+  do {                   \
+    int _rc = (x);       \
+    if (_rc) return _rc; \
+  } while (0)
+
+template <class T>
+static int upload_v(ss_ctx* c, const char* name, const std::vector<T>& v, T** out) {
+  void* p;
+  TRY(pool_get(c, name, sizeof(T) * std::max<size_t>(v.size(), 1), &p));
+  if (!v.empty()) SS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c->stream));
+  *out = (T*)p;
+  return SS_OK;
+}
+
+struct SharedPlan {
+  int npairs = 0;
+  std::vector<int> pi, pk, p1, p2;  // used pairs; per-quartet pair indices
+  int* d_pi = nullptr; int* d_pk = nullptr; int* d_p1 = nullptr; int* d_p2 = nullptr;
+  MixDev mix{};
+};
+
+static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
+  const int n = c->n;
+  std::vector<int> pidx((size_t)n * n, -1);
+  auto use = [&](int i, int k) {
+    int& v = pidx[i + (size_t)n * k];
+    if (v < 0) {
+      v = S.npairs++;
+      S.pi.push_back(i);
+      S.pk.push_back(k);
+    }
+    return v;
+  };
+  S.p1.resize(c->nint);
+  S.p2.resize(c->nint);
+  for (int64_t q = 0; q < c->nint; q++) {
+    S.p1[q] = use(c->h_is[q] - 1, c->h_ks[q] - 1);
+    S.p2[q] = use(c->h_js[q] - 1, c->h_ls[q] - 1);
+  }
+  // mixture: the distinct ZV-map densities (G_ik, c_ik) of the used pairs, equal weights
+  std::vector<double> G, cc;
+  for (int p = 0; p < S.npairs; p++) {
+    int i = S.pi[p], k = S.pk[p];
+    double gi = c->h_gs[i], gk = c->h_gs[k];
+    double g[3], cv = 0.5 * a_zv / (gi + gk);
+    for (int l = 0; l < 3; l++) g[l] = (gi * c->h_center[l + 3 * i] + gk * c->h_center[l + 3 * k]) / (gi + gk);
+    bool dup = false;
+    for (size_t t = 0; t < cc.size() && !dup; t++)
+      dup = fabs(cc[t] - cv) <= 1e-12 * cv && fabs(G[3 * t] - g[0]) <= 1e-12 && fabs(G[3 * t + 1] - g[1]) <= 1e-12 &&
+            fabs(G[3 * t + 2] - g[2]) <= 1e-12;
+    if (!dup) {
+      G.insert(G.end(), g, g + 3);
+      cc.push_back(cv);
+    }
+  }
+  const int m = (int)cc.size();
+  std::vector<double> cdf(m);
+  std::vector<float> Gf(3 * m), inv2c(m), norm(m);
+  const double wgt = 1.0 / m;
+  const double k0 = pow(2.0 * M_PI, 1.5) * 2.0;
+  for (int t = 0; t < m; t++) {
+    cdf[t] = (t == m - 1) ? 1.0 : (t + 1) * wgt;
+    for (int l = 0; l < 3; l++) Gf[3 * t + l] = (float)G[3 * t + l];
+    inv2c[t] = (float)(1.0 / (2.0 * cc[t]));
+    norm[t] = (float)(wgt / (k0 * pow(cc[t], 1.5)));
+  }
+  double *dG, *dc, *dcdf;
+  float *dGf, *di2c, *dn;
+  TRY(upload_v(c, "sh_G", G, &dG));
+  TRY(upload_v(c, "sh_c", cc, &dc));
+  TRY(upload_v(c, "sh_cdf", cdf, &dcdf));
+  TRY(upload_v(c, "sh_Gf", Gf, &dGf));
+  TRY(upload_v(c, "sh_i2c", inv2c, &di2c));
+  TRY(upload_v(c, "sh_norm", norm, &dn));
+  S.mix = MixDev{m, dG, dc, dcdf, dGf, di2c, dn};
+  TRY(upload_v(c, "sh_pi", S.pi, &S.d_pi));
+  TRY(upload_v(c, "sh_pk", S.pk, &S.d_pk));
+  TRY(upload_v(c, "sh_p1", S.p1, &S.d_p1));
+  TRY(upload_v(c, "sh_p2", S.p2, &S.d_p2));
+  return SS_OK;
+}
+
+int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks, int prec, double sigma_target) {
+  if (prec != SS_PREC_SPLIT_BF16) {
+    ss_set_error_msg("shared estimator: only the SPLIT_BF16 precision runs on the device");
+    return SS_ERR_UNSUPPORTED;
+  }
+  SharedPlan SP;
+  TRY(build_shared_plan(c, a_zv, SP));
+  const int P = SP.npairs, n = c->n;
+  const int64_t nint = c->nint;
+  // sub-chunk of samples whose GEMM accumulates in one FP32 TMEM accumulator
+  const int64_t Sc = std::min<int64_t>(npts, 65536);
+  const int64_t Kh = (Sc + 31) / 32 * 32;  // K = 2 Kh is a multiple of 64
+  const int64_t K = 2 * Kh;
+  const int T = (P + 127) / 128;
+  const int64_t ktiles = K / 64;
+  int ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(ktiles, (2 * c->num_sms + T * T - 1) / (T * T)));
+  void* p;
+  double *u1, *u2, *w, *Cblk, *acc, *acc2;
+  float *F, *Cp;
+  __nv_bfloat16 *Ahi, *Alo, *Bhi, *Blo;
+  int* err;
+  TRY(pool_get(c, "sh_u1", sizeof(double) * 3 * Sc, &p)); u1 = (double*)p;
+  TRY(pool_get(c, "sh_u2", sizeof(double) * 3 * Sc, &p)); u2 = (double*)p;
+  TRY(pool_get(c, "sh_w", sizeof(double) * Sc, &p)); w = (double*)p;
+  TRY(pool_get(c, "sh_F", sizeof(float) * 6 * (size_t)n * Sc, &p)); F = (float*)p;
+  const size_t opb = sizeof(__nv_bfloat16) * (size_t)P * K;
+  TRY(pool_get(c, "sh_Ahi", opb, &p)); Ahi = (__nv_bfloat16*)p;
+  TRY(pool_get(c, "sh_Alo", opb, &p)); Alo = (__nv_bfloat16*)p;
+  TRY(pool_get(c, "sh_Bhi", opb, &p)); Bhi = (__nv_bfloat16*)p;
+  TRY(pool_get(c, "sh_Blo", opb, &p)); Blo = (__nv_bfloat16*)p;
+  TRY(pool_get(c, "sh_Cp", sizeof(float) * (size_t)ksplit * P * P, &p)); Cp = (float*)p;
+  TRY(pool_get(c, "sh_Cblk", sizeof(double) * (size_t)P * P, &p)); Cblk = (double*)p;
+  TRY(pool_get(c, "sh_acc", sizeof(double) * nint, &p)); acc = (double*)p;
+  TRY(pool_get(c, "sh_acc2", sizeof(double) * nint, &p)); acc2 = (double*)p;
+  TRY(pool_get(c, "sh_err", sizeof(int), &p)); err = (int*)p;
+  unsigned long long* maxbits;
+  TRY(pool_get(c, "sh_maxbits", sizeof(unsigned long long), &p)); maxbits = (unsigned long long*)p;
+  SS_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(double) * nint, c->stream));
+  SS_CUDA_TRY(cudaMemsetAsync(acc2, 0, sizeof(double) * nint, c->stream));
+  SS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  TRY(dev_alloc(c, c->d_mean, sizeof(double) * nint));
+  TRY(dev_alloc(c, c->d_sigma, sizeof(double) * nint));
+  const int64_t PP = (int64_t)P * P;
+  int done = 0;
+  for (int b = 0; b < nblocks; b++) {
+    SS_CUDA_TRY(cudaMemsetAsync(Cblk, 0, sizeof(double) * PP, c->stream));
+    for (int64_t c0 = 0; c0 < npts; c0 += Sc) {
+      const int64_t ns = std::min(Sc, npts - c0);
+      const int64_t first = (int64_t)b * npts + c0;
+      shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, u1, u2, w);
+      SS_CUDA_TRY(cudaGetLastError());
+      shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)n), 128, 0, c->stream>>>(
+          c->basis, ns, Sc, u1, u2, F);
+      SS_CUDA_TRY(cudaGetLastError());
+      shared_operand_kernel<<<dim3((unsigned)((Kh + 255) / 256), (unsigned)P), 256, 0, c->stream>>>(
+          ns, Kh, Sc, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);
+      SS_CUDA_TRY(cudaGetLastError());
+      TRY(launch_split_bf16_gemm(c->stream, Ahi, Alo, Bhi, Blo, P, K, ksplit, Cp, err));
+      shared_accumulate_block<<<(unsigned)((PP + 255) / 256), 256, 0, c->stream>>>(P, ksplit, Cp, Cblk);
+      SS_CUDA_TRY(cudaGetLastError());
+      c->launches += 5;
+    }
+    shared_block_stats<<<(unsigned)((nint + 255) / 256), 256, 0, c->stream>>>(nint, P, npts, SP.d_p1, SP.d_p2, Cblk,
+                                                                               acc, acc2);
+    SS_CUDA_TRY(cudaGetLastError());
+    c->launches++;
+    done = b + 1;
+    if (sigma_target > 0.0 && done >= 2 && done < nblocks) {
+      SS_CUDA_TRY(cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), c->stream));
+      SS_CUDA_TRY(launch_zv_final(c->stream, nint, done, 1, acc, acc2, (double*)c->d_mean.ptr,
+                                  (double*)c->d_sigma.ptr, maxbits));
+      c->launches++;
+      unsigned long long h = 0;
+      SS_CUDA_TRY(cudaMemcpyAsync(&h, maxbits, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+      SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      double ms;
+      memcpy(&ms, &h, sizeof ms);
+      if (ms <= sigma_target) break;
+    }
+  }
+  SS_CUDA_TRY(cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), c->stream));
+  SS_CUDA_TRY(launch_zv_final(c->stream, nint, done, 1, acc, acc2, (double*)c->d_mean.ptr, (double*)c->d_sigma.ptr,
+                              maxbits));
+  c->launches++;
+  unsigned long long h = 0;
+  int herr = 0;
+  SS_CUDA_TRY(cudaMemcpyAsync(&h, maxbits, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (herr) {
+    ss_set_error_msg("tcgen05 GEMM: a bounded wait gave up (code %d)", herr);
+    return SS_ERR_TIMEOUT;
+  }
+  memcpy(&c->mc_max_sigma, &h, sizeof(double));
+  c->mc_blocks_done = done;
+  c->have_mc = true;
+  return SS_OK;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+__global__ void sum_slices_kernel(int64_t PP, int ksplit, const float* __restrict__ Cp, float* __restrict__ C) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= PP) return;
+  double v = 0.0;
+  for (int t = 0; t < ksplit; t++) v += (double)Cp[t * PP + e];
+  C[e] = (float)v;
+}
+
+extern "C" int ss_split_bf16_gemm(ss_ctx* c, int P, int64_t K, const uint16_t* a_hi, const uint16_t* a_lo,
+                                  const uint16_t* b_hi, const uint16_t* b_lo, int ksplit, float* out) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (P <= 0 || K <= 0 || K % 64 != 0 || !a_hi || !a_lo || !b_hi || !b_lo || !out || ksplit < 0) {
+    ss_set_error_msg("ss_split_bf16_gemm: need P > 0, K a positive multiple of 64, non-null buffers");
+    return SS_ERR_ARG;
+  }
+  const int T = (P + 127) / 128;
+  if (ksplit == 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(K / 64, (2 * c->num_sms + T * T - 1) / (T * T)));
+  const size_t ob = sizeof(uint16_t) * (size_t)P * K;
+  const int64_t PP = (int64_t)P * P;
+  void *ah, *al, *bh, *bl, *cp, *cc, *err;
+  TRY(pool_get(c, "gm_ah", ob, &ah));
+  TRY(pool_get(c, "gm_al", ob, &al));
+  TRY(pool_get(c, "gm_bh", ob, &bh));
+  TRY(pool_get(c, "gm_bl", ob, &bl));
+  TRY(pool_get(c, "gm_cp", sizeof(float) * PP * ksplit, &cp));
+  TRY(pool_get(c, "gm_c", sizeof(float) * PP, &cc));
+  TRY(pool_get(c, "gm_err", sizeof(int), &err));
+  SS_CUDA_TRY(cudaMemcpyAsync(ah, a_hi, ob, cudaMemcpyHostToDevice, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(al, a_lo, ob, cudaMemcpyHostToDevice, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(bh, b_hi, ob, cudaMemcpyHostToDevice, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(bl, b_lo, ob, cudaMemcpyHostToDevice, c->stream));
+  SS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  TRY(launch_split_bf16_gemm(c->stream, ah, al, bh, bl, P, K, ksplit, (float*)cp, (int*)err));
+  sum_slices_kernel<<<(unsigned)((PP + 255) / 256), 256, 0, c->stream>>>(PP, ksplit, (const float*)cp, (float*)cc);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches += 2;
+  int herr = 0;
+  SS_CUDA_TRY(cudaMemcpyAsync(out, cc, sizeof(float) * PP, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (herr) {
+    ss_set_error_msg("tcgen05 GEMM: a bounded wait gave up (code %d)", herr);
+    return SS_ERR_TIMEOUT;
+  }
+  return SS_OK;
+}
+
+extern "C" int ss_shared_samples(ss_ctx* c, double a_zv, uint64_t seed, int64_t first, int64_t S, double* u1,
+                                 double* u2, double* w) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->n || !c->nint) {
+    ss_set_error_msg("basis and quartets must be set first");
+    return SS_ERR_STATE;
+  }
+  if (S <= 0 || first < 0 || !u1 || !u2 || !w || !(a_zv > 0.0)) {
+    ss_set_error_msg("ss_shared_samples: bad arguments");
+    return SS_ERR_ARG;
+  }
+  SharedPlan SP;
+  TRY(build_shared_plan(c, a_zv, SP));
+  void *a, *b, *ww;
+  TRY(pool_get(c, "smp_u1", sizeof(double) * 3 * S, &a));
+  TRY(pool_get(c, "smp_u2", sizeof(double) * 3 * S, &b));
+  TRY(pool_get(c, "smp_w", sizeof(double) * S, &ww));
+  shared_sample_kernel<<<(unsigned)((S + 127) / 128), 128, 0, c->stream>>>(seed, first, S, SP.mix, (double*)a,
+                                                                          (double*)b, (double*)ww);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  SS_CUDA_TRY(cudaMemcpyAsync(u1, a, sizeof(double) * 3 * S, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(u2, b, sizeof(double) * 3 * S, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaMemcpyAsync(w, ww, sizeof(double) * S, cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SS_OK;
+}

@@ -1,0 +1,501 @@
+// ss_api.cu -- context, basis/quartet setup and the analytic-ERI entry points of the C ABI.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "ss_common.cuh"
+#include "ss_context.cuh"
+
+namespace ss {
+size_t eri_smem_bytes(int max_cnt);
+cudaError_t launch_eri_class(int L, dim3 grid, size_t smem, cudaStream_t st, const BasisDev& B,
+                             const PrimPair* pp, const int64_t* off, const int* cnt,
+                             const int64_t* work, int split, const int32_t* is, const int32_t* js,
+                             const int32_t* ks, const int32_t* ls, double* partial);
+__global__ void prim_pair_count(BasisDev B, int npairs, int* cnt);
+__global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* off, PrimPair* out);
+__global__ void eri_finalize(int64_t nint, const int32_t* is, const int32_t* js, const int32_t* ks,
+                             const int32_t* ls, const int64_t* slot, int split, const double* partial,
+                             const double* pre, int n, double* out);
+__global__ void precond_finalize(int n, int split, const double* partial, double* pre);
+}  // namespace ss
+
+static thread_local std::string g_err;
+
+void ss_set_error_msg(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+void ss_set_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  ss_set_error_msg("CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e), cudaGetErrorString(e),
+                   what, file, line);
+}
+
+#define SS_CHECK_CTX(c)                                \
+  do {                                                 \
+    if (!(c)) {                                        \
+      ss_set_error_msg("null ss_ctx");                 \
+      return SS_ERR_ARG;                               \
+    }                                                  \
+    cudaError_t _se = cudaSetDevice((c)->device);      \
+    if (_se != cudaSuccess) {                          \
+      ss_set_cuda_error(_se, "cudaSetDevice", __FILE__, __LINE__); \
+      return SS_ERR_CUDA;                              \
+    }                                                  \
+  } while (0)
+
+namespace ss {
+
+int dev_alloc(ss_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.ptr && b.bytes >= bytes) return SS_OK;
+  size_t old = b.bytes;
+  if (c->budget && c->used - old + bytes > c->budget) {
+    ss_set_error_msg("device allocation of %zu bytes exceeds the context HBM budget (%zu of %zu used)",
+                     bytes, c->used, c->budget);
+    return SS_ERR_NOMEM;
+  }
+  if (b.ptr) {
+    cudaFree(b.ptr);
+    c->used -= old;
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  if (e != cudaSuccess) {
+    b.ptr = nullptr;
+    ss_set_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+    return SS_ERR_NOMEM;
+  }
+  b.bytes = bytes;
+  c->used += bytes;
+  return SS_OK;
+}
+
+void dev_free(ss_ctx* c, DevBuf& b) {
+  if (b.ptr) {
+    cudaFree(b.ptr);
+    c->used -= b.bytes;
+  }
+  b.ptr = nullptr;
+  b.bytes = 0;
+}
+
+int h2d(ss_ctx* c, DevBuf& b, const void* src, size_t bytes) {
+  int rc = dev_alloc(c, b, bytes);
+  if (rc) return rc;
+  SS_CUDA_TRY(cudaMemcpyAsync(b.ptr, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  return SS_OK;
+}
+
+// per-axis maximum of (power of f1 + power of f2) over the cartesian components of the fits
+static int pair_L(const ss_ctx* c, int f1, int f2) {
+  int L = 0;
+  for (int ax = 0; ax < 3; ax++) {
+    int a = c->h_npower[3 * f1 + ax] + (c->h_itype[f1] == 2 ? 2 : 0);
+    int b = c->h_npower[3 * f2 + ax] + (c->h_itype[f2] == 2 ? 2 : 0);
+    L = std::max(L, a + b);
+  }
+  return L;
+}
+
+static int total_pow(const ss_ctx* c, int f) {
+  return c->h_npower[3 * f] + c->h_npower[3 * f + 1] + c->h_npower[3 * f + 2] +
+         (c->h_itype[f] == 2 ? 2 : 0);
+}
+
+// Run the ERI kernels for the quartets listed in (qis..qls) restricted to `sel` (indices into
+// them); partial sums are written to d_scratch_b and slot[q] gives the partial row of q.
+static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const int32_t* d_qks,
+                   const int32_t* d_qls, const std::vector<int32_t>& qis, const std::vector<int32_t>& qjs,
+                   const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
+                   const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out) {
+  // bucket by class L = max(bra L, ket L)
+  std::vector<std::vector<int64_t>> bucket(SS_MAX_POW + 1);
+  for (int64_t t : sel) {
+    int i = qis[t] - 1, k = qks[t] - 1, j = qjs[t] - 1, l = qls[t] - 1;
+    int L = std::max(pair_L(c, i, k), pair_L(c, j, l));
+    bucket[L].push_back(t);
+  }
+  int64_t nsel = (int64_t)sel.size();
+  // one split for all classes keeps the slot arithmetic simple
+  const int target = c->num_sms * 8;
+  int split = (int)std::min<int64_t>(16, std::max<int64_t>(1, (target + std::max<int64_t>(nsel, 1) - 1) /
+                                                             std::max<int64_t>(nsel, 1)));
+  split_out = split;
+  std::vector<int64_t> work;
+  work.reserve(nsel);
+  std::vector<int64_t> begin(SS_MAX_POW + 1), count(SS_MAX_POW + 1);
+  std::vector<int> maxk(SS_MAX_POW + 1, 0);
+  slot_of_sel.assign(qis.size(), -1);
+  for (int L = 0; L <= SS_MAX_POW; L++) {
+    begin[L] = (int64_t)work.size();
+    for (int64_t t : bucket[L]) {
+      slot_of_sel[t] = (int64_t)work.size();
+      work.push_back(t);
+      int j = qjs[t] - 1, l = qls[t] - 1;
+      maxk[L] = std::max(maxk[L], c->h_pp_cnt[ss_pair_index(j, l)]);
+    }
+    count[L] = (int64_t)work.size() - begin[L];
+  }
+  int rc = h2d(c, c->d_scratch_a, work.data(), sizeof(int64_t) * std::max<size_t>(work.size(), 1));
+  if (rc) return rc;
+  rc = dev_alloc(c, c->d_scratch_b, sizeof(double) * std::max<int64_t>(nsel * split, 1));
+  if (rc) return rc;
+  const int64_t* d_work = (const int64_t*)c->d_scratch_a.ptr;
+  double* d_partial = (double*)c->d_scratch_b.ptr;
+  for (int L = 0; L <= SS_MAX_POW; L++) {
+    if (!count[L]) continue;
+    size_t smem = eri_smem_bytes(std::max(maxk[L], 1));
+    // grid.x is limited to 2^31-1: launch in chunks of quartets
+    const int64_t chunk = (int64_t)(2147483647 / split);
+    for (int64_t s0 = 0; s0 < count[L]; s0 += chunk) {
+      int64_t nq = std::min(chunk, count[L] - s0);
+      dim3 grid((unsigned)(nq * split));
+      cudaError_t e = launch_eri_class(L, grid, smem, c->stream, c->basis, (const PrimPair*)c->d_pp.ptr,
+                                       (const int64_t*)c->d_pp_off.ptr, (const int*)c->d_pp_cnt.ptr,
+                                       d_work + begin[L] + s0, split, d_qis, d_qjs, d_qks, d_qls,
+                                       d_partial + (begin[L] + s0) * split);
+      if (e != cudaSuccess) {
+        ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
+        return SS_ERR_CUDA;
+      }
+      c->launches++;
+    }
+  }
+  return SS_OK;
+}
+
+int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out) {
+  DevBuf& b = c->pool[name];
+  int rc = dev_alloc(c, b, bytes);
+  if (rc) return rc;
+  *out = b.ptr;
+  return SS_OK;
+}
+
+int ensure_precond(ss_ctx* c) {
+  if (c->have_precond) return SS_OK;
+  if (!c->n) {
+    ss_set_error_msg("no basis set");
+    return SS_ERR_STATE;
+  }
+  // diagonal quartets (ik|ik), i >= k, in pair-index order (src/two_e_slater.F90:230-236)
+  int n = c->n;
+  int64_t np = (int64_t)n * (n + 1) / 2;
+  std::vector<int32_t> qi(np), qk(np);
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k <= i; k++) {
+      int64_t p = ss_pair_index(i, k);
+      qi[p] = i + 1;
+      qk[p] = k + 1;
+    }
+  DevBuf di, dk;
+  int rc = h2d(c, di, qi.data(), sizeof(int32_t) * np);
+  if (!rc) rc = h2d(c, dk, qk.data(), sizeof(int32_t) * np);
+  std::vector<int64_t> sel(np), slot;
+  std::iota(sel.begin(), sel.end(), 0);
+  int split = 1;
+  if (!rc)
+    rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split);
+  if (rc) {
+    dev_free(c, di);
+    dev_free(c, dk);
+    return rc;
+  }
+  // slots are a permutation of pair indices: gather partials back into pair order on the host side
+  // by re-sorting (cheap: np entries)
+  std::vector<double> part((size_t)np * split);
+  rc = dev_alloc(c, c->d_precond, sizeof(double) * n * n);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(part.data(), c->d_scratch_b.ptr, sizeof(double) * np * split,
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  dev_free(c, di);
+  dev_free(c, dk);
+  if (e != cudaSuccess) {
+    ss_set_cuda_error(e, "precond copy", __FILE__, __LINE__);
+    return SS_ERR_CUDA;
+  }
+  c->h_precond.assign((size_t)n * n, 0.0);
+  for (int64_t p = 0; p < np; p++) {
+    double v = 0.0;
+    for (int t = 0; t < split; t++) v = v + part[slot[p] * split + t];
+    int i = qi[p] - 1, k = qk[p] - 1;
+    c->h_precond[i + (size_t)n * k] = v;
+    c->h_precond[k + (size_t)n * i] = v;
+  }
+  SS_CUDA_TRY(cudaMemcpyAsync(c->d_precond.ptr, c->h_precond.data(), sizeof(double) * n * n,
+                              cudaMemcpyHostToDevice, c->stream));
+  c->have_precond = true;
+  return SS_OK;
+}
+
+int ensure_gauss(ss_ctx* c) {
+  if (c->have_gauss) return SS_OK;
+  if (!c->nint) {
+    ss_set_error_msg("no quartets set");
+    return SS_ERR_STATE;
+  }
+  int rc = ensure_precond(c);
+  if (rc) return rc;
+  const int n = c->n;
+  const double seuil = 1.e-15;  // src/two_e_slater.F90:13
+  std::vector<int64_t> sel;
+  sel.reserve(c->nint);
+  int64_t nzero = 0;
+  for (int64_t q = 0; q < c->nint; q++) {
+    int i = c->h_is[q] - 1, k = c->h_ks[q] - 1, j = c->h_js[q] - 1, l = c->h_ls[q] - 1;
+    double pik = c->h_precond[i + (size_t)n * k], pjl = c->h_precond[j + (size_t)n * l];
+    bool small = fabs(pik * pjl) < seuil * seuil;
+    if (small) nzero++;
+    if (i == j && k == l) continue;
+    if (!small) sel.push_back(q);
+  }
+  c->n_removed = nzero;
+  std::vector<int64_t> slot;
+  int split = 1;
+  rc = run_eri(c, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+               (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, split);
+  if (rc) return rc;
+  rc = h2d(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
+  if (rc) return rc;
+  rc = dev_alloc(c, c->d_gauss, sizeof(double) * c->nint);
+  if (rc) return rc;
+  int64_t nb = (c->nint + 255) / 256;
+  eri_finalize<<<(unsigned)nb, 256, 0, c->stream>>>(
+      c->nint, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+      (const int32_t*)c->d_ls.ptr, (const int64_t*)c->d_scratch_c.ptr, split,
+      (const double*)c->d_scratch_b.ptr, (const double*)c->d_precond.ptr, n, (double*)c->d_gauss.ptr);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  c->have_gauss = true;
+  return SS_OK;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+const char* ss_strerror(int code) {
+  switch (code) {
+    case SS_OK: return "ok";
+    case SS_ERR_ARG: return "invalid argument";
+    case SS_ERR_STATE: return "call out of order";
+    case SS_ERR_CUDA: return "CUDA runtime error";
+    case SS_ERR_NOMEM: return "out of device memory or over the HBM budget";
+    case SS_ERR_UNSUPPORTED: return "input outside the kernels' limits";
+    case SS_ERR_TIMEOUT: return "bounded device wait timed out";
+    case SS_ERR_NUMERIC: return "non-finite result";
+    default: return "unknown error";
+  }
+}
+
+const char* ss_last_error(void) { return g_err.c_str(); }
+
+ss_ctx* ss_create(int device, size_t hbm_budget) {
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) {
+    ss_set_cuda_error(e, "cudaGetDeviceCount", __FILE__, __LINE__);
+    return nullptr;
+  }
+  if (device < 0 || device >= ndev) {
+    ss_set_error_msg("device %d out of range (%d devices)", device, ndev);
+    return nullptr;
+  }
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    ss_set_cuda_error(e, "cudaSetDevice", __FILE__, __LINE__);
+    return nullptr;
+  }
+  ss_ctx* c = new ss_ctx();
+  c->device = device;
+  c->budget = hbm_budget;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (c->num_sms <= 0) c->num_sms = 152;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    ss_set_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+
+void ss_destroy(ss_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->d_center, &c->d_npower, &c->d_nsto, &c->d_itype, &c->d_ng, &c->d_cg, &c->d_gg,
+                    &c->d_gs, &c->d_pp, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
+                    &c->d_ls, &c->d_precond, &c->d_gauss, &c->d_mean, &c->d_sigma, &c->d_scratch_a,
+                    &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d};
+  for (DevBuf* b : bufs) dev_free(c, *b);
+  for (auto& kv : c->pool) dev_free(c, kv.second);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int64_t ss_launch_count(const ss_ctx* c) { return c ? c->launches : -1; }
+
+int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower, const int* n_sto,
+                 const int* i_type, const int* n_gauss, const double* c_gauss, int ld,
+                 const double* g_gauss, const double* g_slater) {
+  SS_CHECK_CTX(c);
+  if (nbasis <= 0 || ld <= 0 || !center || !npower || !n_sto || !i_type || !n_gauss || !c_gauss ||
+      !g_gauss || !g_slater) {
+    ss_set_error_msg("ss_basis_set: bad arguments (nbasis=%d ld=%d)", nbasis, ld);
+    return SS_ERR_ARG;
+  }
+  for (int i = 0; i < nbasis; i++) {
+    if (n_gauss[i] < 1 || n_gauss[i] > ld || n_gauss[i] > SS_MAX_NG) {
+      ss_set_error_msg("function %d: n_gauss=%d outside 1..min(ld=%d,%d)", i + 1, n_gauss[i], ld, SS_MAX_NG);
+      return SS_ERR_ARG;
+    }
+    if (i_type[i] == 3) {  // the reference stops here too (src/build_c_g_gauss_STO.F90:27)
+      ss_set_error_msg("function %d: i_type=3 is not supported", i + 1);
+      return SS_ERR_UNSUPPORTED;
+    }
+    if (i_type[i] != 1 && i_type[i] != 2) {
+      ss_set_error_msg("function %d: invalid i_type=%d", i + 1, i_type[i]);
+      return SS_ERR_ARG;
+    }
+    for (int ax = 0; ax < 3; ax++)
+      if (npower[3 * i + ax] < 0) {
+        ss_set_error_msg("function %d: negative power", i + 1);
+        return SS_ERR_ARG;
+      }
+    if (!(g_slater[i] > 0.0)) {
+      ss_set_error_msg("function %d: zeta must be > 0", i + 1);
+      return SS_ERR_ARG;
+    }
+  }
+  c->n = nbasis;
+  c->ld = ld;
+  c->h_center.assign(center, center + 3 * nbasis);
+  c->h_npower.assign(npower, npower + 3 * nbasis);
+  c->h_nsto.assign(n_sto, n_sto + nbasis);
+  c->h_itype.assign(i_type, i_type + nbasis);
+  c->h_ng.assign(n_gauss, n_gauss + nbasis);
+  c->h_cg.assign(c_gauss, c_gauss + (size_t)ld * nbasis * 2);
+  c->h_gg.assign(g_gauss, g_gauss + (size_t)ld * nbasis);
+  c->h_gs.assign(g_slater, g_slater + nbasis);
+  for (int i = 0; i < nbasis; i++)
+    for (int k = 0; k <= i; k++)
+      if (pair_L(c, i, k) > SS_MAX_POW) {
+        ss_set_error_msg("functions %d,%d: per-axis angular power %d exceeds the kernel limit %d "
+                         "(s, p, d and r^2-type s fits are supported)", i + 1, k + 1, pair_L(c, i, k), SS_MAX_POW);
+        c->n = 0;
+        return SS_ERR_UNSUPPORTED;
+      }
+  int rc = 0;
+  rc |= h2d(c, c->d_center, center, sizeof(double) * 3 * nbasis);
+  rc |= h2d(c, c->d_npower, npower, sizeof(int) * 3 * nbasis);
+  rc |= h2d(c, c->d_nsto, n_sto, sizeof(int) * nbasis);
+  rc |= h2d(c, c->d_itype, i_type, sizeof(int) * nbasis);
+  rc |= h2d(c, c->d_ng, n_gauss, sizeof(int) * nbasis);
+  rc |= h2d(c, c->d_cg, c_gauss, sizeof(double) * ld * nbasis * 2);
+  rc |= h2d(c, c->d_gg, g_gauss, sizeof(double) * ld * nbasis);
+  rc |= h2d(c, c->d_gs, g_slater, sizeof(double) * nbasis);
+  if (rc) return SS_ERR_NOMEM;
+  c->basis = BasisDev{nbasis, ld, (const double*)c->d_center.ptr, (const int*)c->d_npower.ptr,
+                      (const int*)c->d_nsto.ptr, (const int*)c->d_itype.ptr, (const int*)c->d_ng.ptr,
+                      (const double*)c->d_cg.ptr, (const double*)c->d_gg.ptr, (const double*)c->d_gs.ptr};
+  // primitive-pair tables
+  int npairs = nbasis * (nbasis + 1) / 2;
+  rc = dev_alloc(c, c->d_pp_cnt, sizeof(int) * npairs);
+  if (rc) return rc;
+  prim_pair_count<<<npairs, 128, 0, c->stream>>>(c->basis, npairs, (int*)c->d_pp_cnt.ptr);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  c->h_pp_cnt.assign(npairs, 0);
+  SS_CUDA_TRY(cudaMemcpyAsync(c->h_pp_cnt.data(), c->d_pp_cnt.ptr, sizeof(int) * npairs,
+                              cudaMemcpyDeviceToHost, c->stream));
+  SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->h_pp_off.assign(npairs + 1, 0);
+  for (int p = 0; p < npairs; p++) c->h_pp_off[p + 1] = c->h_pp_off[p] + c->h_pp_cnt[p];
+  rc = h2d(c, c->d_pp_off, c->h_pp_off.data(), sizeof(int64_t) * (npairs + 1));
+  if (rc) return rc;
+  rc = dev_alloc(c, c->d_pp, sizeof(PrimPair) * std::max<int64_t>(c->h_pp_off[npairs], 1));
+  if (rc) return rc;
+  prim_pair_fill<<<npairs, 32, 0, c->stream>>>(c->basis, npairs, (const int64_t*)c->d_pp_off.ptr,
+                                               (PrimPair*)c->d_pp.ptr);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  c->have_precond = c->have_gauss = c->have_mc = false;
+  return SS_OK;
+}
+
+int ss_quartets_set(ss_ctx* c, int64_t nint, const int32_t* is, const int32_t* js, const int32_t* ks,
+                    const int32_t* ls) {
+  SS_CHECK_CTX(c);
+  if (!c->n) {
+    ss_set_error_msg("ss_quartets_set before ss_basis_set");
+    return SS_ERR_STATE;
+  }
+  if (nint < 0 || (nint > 0 && (!is || !js || !ks || !ls))) {
+    ss_set_error_msg("ss_quartets_set: bad arguments");
+    return SS_ERR_ARG;
+  }
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q], j = js[q], k = ks[q], l = ls[q];
+    if (i < 1 || j < 1 || k < 1 || l < 1 || i > c->n || j > c->n || k > c->n || l > c->n || i < k || j < l) {
+      ss_set_error_msg("quartet %lld: (%d,%d,%d,%d) needs 1 <= k <= i <= n and 1 <= l <= j <= n",
+                       (long long)q + 1, i, j, k, l);
+      return SS_ERR_ARG;
+    }
+  }
+  c->nint = nint;
+  c->h_is.assign(is, is + nint);
+  c->h_js.assign(js, js + nint);
+  c->h_ks.assign(ks, ks + nint);
+  c->h_ls.assign(ls, ls + nint);
+  int rc = 0;
+  size_t b = sizeof(int32_t) * std::max<int64_t>(nint, 1);
+  rc |= h2d(c, c->d_is, is, sizeof(int32_t) * nint);
+  rc |= h2d(c, c->d_js, js, sizeof(int32_t) * nint);
+  rc |= h2d(c, c->d_ks, ks, sizeof(int32_t) * nint);
+  rc |= h2d(c, c->d_ls, ls, sizeof(int32_t) * nint);
+  (void)b;
+  if (rc) return SS_ERR_NOMEM;
+  c->have_gauss = c->have_mc = false;
+  return SS_OK;
+}
+
+int ss_precond(ss_ctx* c, double* precond) {
+  SS_CHECK_CTX(c);
+  int rc = ensure_precond(c);
+  if (rc) return rc;
+  if (precond) memcpy(precond, c->h_precond.data(), sizeof(double) * c->n * c->n);
+  return SS_OK;
+}
+
+int ss_gauss_eri(ss_ctx* c, double* out, int64_t* n_removed) {
+  SS_CHECK_CTX(c);
+  int rc = ensure_gauss(c);
+  if (rc) return rc;
+  if (out) {
+    SS_CUDA_TRY(cudaMemcpyAsync(out, c->d_gauss.ptr, sizeof(double) * c->nint, cudaMemcpyDeviceToHost,
+                                c->stream));
+  }
+  SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (n_removed) *n_removed = c->n_removed;
+  return SS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// ss_common.cuh -- shared definitions for the sm_103a kernels of the two-electron path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/slaterstoch.h"
+
+#define SS_CUDA_TRY(expr)                          \
+  do {                                             \
+    cudaError_t _e = (expr);                       \
+    if (_e != cudaSuccess) {                       \
+      ss_set_cuda_error(_e, #expr, __FILE__, __LINE__); \
+      return SS_ERR_CUDA;                          \
+    }                                              \
+  } while (0)
+
+void ss_set_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+void ss_set_error_msg(const char* fmt, ...);
+
+namespace ss {
+
+// Limits of the device kernels (checked on the host before any launch).
+constexpr int SS_MAX_POW = 4;        // per-function per-axis power, incl. the +2 of r^2 fits
+constexpr int SS_MAX_NG = 30;        // Gaussians per fit (src/common_data.F90:7)
+constexpr int SS_MAX_NF = 24;        // highest Boys order F_n used by one primitive quartet
+
+// One primitive pair of a function pair (i,k): the Gaussian product of
+// g_gauss(m1,i) and g_gauss(m2,k) (src/gaussian_product.F90:1-33), padded to 128 bytes.
+struct __align__(16) PrimPair {
+  double p, p_inv;       // alpha+beta, 1/(alpha+beta)
+  double P[3];           // product centre
+  double fact;           // K_AB (0 pairs are not stored)
+  double coef;           // c(m1,i) * c(m2,k)
+  double PA[3];          // P - A  (pows_a(1) of src/give_explicit_poly_and_gaussian.F90:125)
+  double PB[3];          // P - B
+  double pad[3];
+};
+
+// Device view of the fitted basis (Fortran layouts, 0-based).
+struct BasisDev {
+  int n, ld;
+  const double* center;   // [3n]
+  const int* npower;      // [3n]
+  const int* n_sto;       // [n]
+  const int* i_type;      // [n]
+  const int* n_gauss;     // [n]
+  const double* c_gauss;  // [ld*n*2]
+  const double* g_gauss;  // [ld*n]
+  const double* g_slater; // [n]
+};
+
+__host__ __device__ inline int64_t ss_pair_index(int i, int k) {  // i >= k, 0-based
+  return (int64_t)i * (i + 1) / 2 + k;
+}
+
+}  // namespace ss

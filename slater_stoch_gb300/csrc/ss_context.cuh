@@ -1,0 +1,91 @@
+// ss_context.cuh -- the ss_ctx object behind the C ABI (device-resident job state).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ss_common.cuh"
+
+namespace ss {
+
+// A device allocation tracked against the context's HBM budget.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct EriPlan {
+  // one entry per (class L) bucket; work lists hold quartet indices
+  std::vector<int> L;
+  std::vector<int64_t> begin, count;  // into work[]
+  std::vector<int> split;
+  std::vector<int64_t> partial_begin;  // into partial[]
+  std::vector<int> max_ket;            // largest ket primitive-pair count in the bucket
+  int64_t total_partial = 0;
+};
+
+// Parameters of the shared-walker proposal: a mixture of ZV-map densities
+// p_c(u) = exp(-|u-G_c|/(2 c_c)) / ((2 pi)^{3/2} 2 c_c^{3/2} |u-G_c|^{3/2}).
+struct Mixture {
+  int m = 0;
+  std::vector<double> G;       // 3*m
+  std::vector<double> c;       // m
+  std::vector<double> weight;  // m, sums to 1
+  std::vector<double> cdf;     // m
+};
+
+}  // namespace ss
+
+struct ss_ctx {
+  int device = 0;
+  size_t budget = 0, used = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  int num_sms = 0;
+
+  // basis (device copies)
+  int n = 0, ld = 0;
+  std::vector<double> h_center, h_gg, h_cg, h_gs;
+  std::vector<int> h_npower, h_nsto, h_itype, h_ng;
+  ss::DevBuf d_center, d_npower, d_nsto, d_itype, d_ng, d_cg, d_gg, d_gs;
+  ss::BasisDev basis{};
+
+  // primitive pairs
+  ss::DevBuf d_pp, d_pp_off, d_pp_cnt;
+  std::vector<int> h_pp_cnt;
+  std::vector<int64_t> h_pp_off;
+
+  // quartets
+  int64_t nint = 0;
+  std::vector<int32_t> h_is, h_js, h_ks, h_ls;
+  ss::DevBuf d_is, d_js, d_ks, d_ls;
+
+  // analytic results
+  bool have_precond = false, have_gauss = false;
+  std::vector<double> h_precond;
+  ss::DevBuf d_precond, d_gauss;
+  int64_t n_removed = 0;
+
+  // MC results
+  bool have_mc = false;
+  ss::DevBuf d_mean, d_sigma;
+
+  // scratch reused across calls
+  ss::DevBuf d_scratch_a, d_scratch_b, d_scratch_c, d_scratch_d;
+  // named device buffers of the MC and cleanup stages
+  std::map<std::string, ss::DevBuf> pool;
+  int mc_blocks_done = 0;
+  double mc_max_sigma = 0.0;
+};
+
+namespace ss {
+int dev_alloc(ss_ctx* c, DevBuf& b, size_t bytes);   // (re)allocates only when growing
+void dev_free(ss_ctx* c, DevBuf& b);
+int h2d(ss_ctx* c, DevBuf& b, const void* src, size_t bytes);
+int ensure_precond(ss_ctx* c);
+// named pool buffer of at least `bytes`; *out receives the device pointer
+int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out);
+int ensure_gauss(ss_ctx* c);
+}  // namespace ss

@@ -1,0 +1,109 @@
+"""Host-side logic: input readers, basis construction, quartet map, C-ABI surface (no GPU)."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from slater_stoch_gb300 import basis, configs, perfmodel
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_fit_table_complete():
+    c, g = basis.load_fit_tables()
+    for n in range(1, 31):
+        assert np.all(c[n, 1:n + 1] != 0) and np.all(g[n, 1:n + 1] > 0)
+    # SMILES 1-Gaussian fit of exp(-r) (first entry of the table)
+    assert c[1, 1] == 0.7709254 and g[1, 1] == 0.6070177
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 26])
+def test_mapping_count_and_order(n):
+    is_, js, ks, ls = basis.build_mapping(n)
+    P = n * (n + 1) // 2
+    assert len(is_) == P * (P + 1) // 2
+    assert np.all(is_ >= ks) and np.all(js >= ls) and np.all(is_ >= js)
+    assert not np.any((is_ == js) & (ls > ks))
+    # every unordered pair-of-pairs appears exactly once
+    seen = set()
+    for i, j, k, l in zip(is_, js, ks, ls):
+        a, b = (int(i), int(k)), (int(j), int(l))
+        key = (min(a, b), max(a, b))
+        assert key not in seen
+        seen.add(key)
+
+
+def test_configs_sizes():
+    b1 = configs.h2o_minimal()
+    b2 = configs.h2o_26()
+    assert b1.n == 7 and b2.n == 26
+    assert perfmodel.primitive_quartets(b1, basis.build_mapping(7)) == pytest.approx(1.968e8, rel=1e-3)
+    assert perfmodel.primitive_quartets(b2, basis.build_mapping(26)) == pytest.approx(1.78253e10, rel=1e-4)
+    b3 = configs.random_molecule(seed=3)
+    assert 50 <= b3.n <= 132
+
+
+def test_basis_fit_coefficients_type2():
+    # 2S: c2 = 2 c_fit g_fit zeta, g = zeta^2 g_fit (src/build_c_g_gauss_STO.F90:16-26)
+    c, g = basis.load_fit_tables()
+    b = configs.h2o_minimal(ng0=20)
+    i = b.names.index("O1:2S")
+    z = 2.25
+    np.testing.assert_allclose(b.c_gauss[1, i, :20], 2 * c[20, 1:21] * g[20, 1:21] * z, rtol=0, atol=0)
+    np.testing.assert_allclose(b.g_gauss[i, :20], z * z * g[20, 1:21], rtol=0, atol=0)
+    assert b.i_type[i] == 2 and np.all(b.c_gauss[0, i] == 0)
+
+
+def test_read_inputs(tmp_path):
+    (tmp_path / "h2o.xyz").write_text("3\nWater\nO 0. 0. 0.\nH 0.0 0.756988 0.587016\nH 0.0 -0.756988 0.587016\n")
+    (tmp_path / "VB").write_text("H 1S 1.24\nO 1S 7.66\nO 2S 2.25\nO 2P 2.25\n")
+    (tmp_path / "j_in").write_text("Simulation number\n1\nMolecule\nh2o\nbasis\nVB\nNg\n 20 0 0 1.d30 0\n"
+                                   "npts\n 4000\n****\nZV\n1.8\n")
+    cfg = basis.read_j_in(tmp_path / "j_in")
+    assert cfg["npts_two_elec"] == 4000 and cfg["a_zv"] == 1.8 and cfg["fit"].ng0 == 20
+    mol = basis.read_geometry(tmp_path / "h2o.xyz")
+    np.testing.assert_allclose(mol.coords[1], [0.0, 1.4305, 1.1093], atol=2e-5)
+    b = basis.build_basis(mol, basis.read_basis(tmp_path / "VB"), cfg["fit"])
+    assert b.n == 7
+
+
+def test_j_in_rejects_npts_not_multiple_of_nw(tmp_path):
+    (tmp_path / "j_in").write_text("t\n1\nt\nh2o\nt\nVB\nt\n 4 0 0 4. 0\nt\n 4001\nt\nt\n1.8\n")
+    with pytest.raises(ValueError):
+        basis.read_j_in(tmp_path / "j_in")
+
+
+def test_unknown_atom_rejected():
+    with pytest.raises(ValueError):
+        basis.element_number("Xx")
+
+
+def test_header_symbols_exported():
+    """libslaterstoch.so (built for sm_103a here by nvcc) exports every function of the header."""
+    from slater_stoch_gb300 import build
+    lib = build.build()
+    hdr = (ROOT / "include" / "slaterstoch.h").read_text()
+    decl = set(re.findall(r"\b(ss_[a-z0-9_]+)\s*\(", hdr))
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (ss_[a-z0-9_]+)\b", out))
+    assert decl and decl <= exported, decl - exported
+    from slater_stoch_gb300 import _lib
+    assert set(_lib.SIGNATURES) == decl
+
+
+def test_library_loads_without_gpu():
+    """The ABI loads on a GPU-less host and reports the missing device instead of crashing."""
+    from slater_stoch_gb300 import _lib
+    L = _lib.load()
+    h = L.ss_create(0, 0)
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        assert not h and L.ss_last_error()
+    elif h:
+        L.ss_destroy(h)
