@@ -124,6 +124,19 @@ void* ss_stream(ss_ctx* ctx);
 int ss_split_bf16_gemm(ss_ctx* ctx, int P, int64_t K, const uint16_t* a_hi, const uint16_t* a_lo,
                        const uint16_t* b_hi, const uint16_t* b_lo, int ksplit, float* c);
 
+/* No counterpart in the reference.  The same contraction for callers that cannot allocate
+ * device memory (their device memory belongs to their own pool, or cudaMalloc is not allowed
+ * where they run): it allocates nothing and needs no ss_ctx.  All pointers are DEVICE pointers
+ * owned by the caller (A*, B* (P,K) BF16 bits, C (P,P) FP32); stream is a cudaStream_t (NULL =
+ * default stream) and the call returns after the stream has finished the work.  The K-slice
+ * partials go to a fixed 16 MiB device array inside the library, so P <= 2048 (larger P is
+ * rejected with SS_ERR_ARG) and ksplit is reduced to fit.  The first call on a device looks up
+ * that array's address; make it before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (other threads, other streams) race and must be serialised. */
+int ss_split_bf16_gemm_noalloc(void* stream, int P, int64_t K, const uint16_t* a_hi,
+                               const uint16_t* a_lo, const uint16_t* b_hi, const uint16_t* b_lo,
+                               int ksplit, float* c);
+
 /* PSD cleanup by randomized SVD deflation (replaces svd_clean, src/svd_clean.F90:1-426).
  * moy (nint) in/out; rank, q as in src/two_e_slater.F90:565-567 (oversample added to rank);
  * seed drives the Gaussian test matrices.  n_removed receives the removed negative components. */

@@ -47,6 +47,8 @@ SIGNATURES = {
     "ss_stream": (C.c_void_p, [C.c_void_p]),
     "ss_split_bf16_gemm": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, u16p, u16p, u16p, u16p, C.c_int,
                                      f32p]),
+    "ss_split_bf16_gemm_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "ss_psd_clean": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                C.c_void_p]),
     "ss_davidson": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,

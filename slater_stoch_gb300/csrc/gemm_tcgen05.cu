@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "shared.cuh"
@@ -259,6 +260,97 @@ int make_map(CUtensorMap* m, const void* base, int rows, int64_t K) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of the contraction.
+//
+// Callers that cannot allocate device memory (an application that hands all of its device
+// memory to its own pool, or code running where cudaMalloc is not allowed) still need the
+// FP32 partial products of the K slices somewhere.  They live in this fixed file-scope device
+// array, which every GPU that loads the library holds until the process exits.  Host code
+// must not pass the symbol itself to a kernel (on the host it is only a stand-in); its device
+// address is looked up once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------------------
+constexpr size_t NOALLOC_FLAG_BYTES = 256;                 // bounded-wait error flag
+constexpr size_t NOALLOC_PARTIAL_BYTES = (size_t)16 << 20;  // 16 MiB of FP32 K-slice partials
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_FLAG_BYTES + NOALLOC_PARTIAL_BYTES];
+
+__global__ void noalloc_sum_slices(int64_t PP, int ksplit, const float* __restrict__ Cp, float* __restrict__ C) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= PP) return;
+  double v = 0.0;
+  for (int t = 0; t < ksplit; t++) v += (double)Cp[t * PP + e];
+  C[e] = (float)v;
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+}  // namespace
+
+int launch_split_bf16_gemm(cudaStream_t st, const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo,
+                           int P, int64_t K, int ksplit, float* c_partial, int* err_flag);
+
+}  // namespace ss
+
+extern "C" int ss_split_bf16_gemm_noalloc(void* stream, int P, int64_t K, const uint16_t* a_hi, const uint16_t* a_lo,
+                                          const uint16_t* b_hi, const uint16_t* b_lo, int ksplit, float* c) {
+  using namespace ss;
+  if (P <= 0 || K <= 0 || K % 64 != 0 || !a_hi || !a_lo || !b_hi || !b_lo || !c || ksplit < 0) {
+    ss_set_error_msg("ss_split_bf16_gemm_noalloc: need P > 0, K a positive multiple of 64, device buffers");
+    return SS_ERR_ARG;
+  }
+  const size_t cap = NOALLOC_PARTIAL_BYTES / sizeof(float);  // floats of partial products
+  const size_t PP = (size_t)P * P;
+  if (PP > cap) {
+    ss_set_error_msg("ss_split_bf16_gemm_noalloc: P=%d needs %zu bytes of partials, more than the fixed "
+                     "%zu-byte scratch (P <= 2048)", P, PP * sizeof(float), NOALLOC_PARTIAL_BYTES);
+    return SS_ERR_ARG;
+  }
+  const int T = (P + 127) / 128;
+  int dev = 0;
+  SS_CUDA_TRY(cudaGetDevice(&dev));
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ksplit == 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(K / 64, (2 * sms + T * T - 1) / (T * T)));
+  ksplit = (int)std::min<size_t>((size_t)ksplit, cap / PP);
+  if (dev < 0 || dev >= 64) {
+    ss_set_error_msg("ss_split_bf16_gemm_noalloc: device %d out of range", dev);
+    return SS_ERR_ARG;
+  }
+  void* base;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {  // first call on this device: look up the array's device address
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        ss_set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+        return SS_ERR_CUDA;
+      }
+      g_noalloc_ptr[dev] = p;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int* err = (int*)base;
+  float* partial = (float*)((unsigned char*)base + NOALLOC_FLAG_BYTES);
+  SS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));  // the flag must start at zero
+  int rc = launch_split_bf16_gemm(st, a_hi, a_lo, b_hi, b_lo, P, K, ksplit, partial, err);
+  if (rc) return rc;
+  noalloc_sum_slices<<<(unsigned)((PP + 255) / 256), 256, 0, st>>>((int64_t)PP, ksplit, partial, c);
+  SS_CUDA_TRY(cudaGetLastError());
+  int herr = 0;
+  SS_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    ss_set_error_msg("tcgen05 GEMM: a bounded wait gave up (code %d)", herr);
+    return SS_ERR_TIMEOUT;
+  }
+  return SS_OK;
+}
+
+namespace ss {
 
 int launch_split_bf16_gemm(cudaStream_t st, const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo,
                            int P, int64_t K, int ksplit, float* c_partial, int* err_flag) {
