@@ -1,0 +1,14 @@
+// eri_k2t.cu -- eri_kernel<2, true> (own translation unit: the classes compile in parallel).
+#include "eri_kernel.cuh"
+
+namespace ss {
+cudaError_t launch_eri_L2t(dim3 grid, int ktile, size_t smem, cudaStream_t st, const BasisDev& B,
+                              const PrimPair* pp, const int64_t* off, const int* cnt, const int64_t* work,
+                              int split, const int32_t* is, const int32_t* js, const int32_t* ks,
+                              const int32_t* ls, double* partial) {
+  cudaError_t e = cudaFuncSetAttribute(eri_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  eri_kernel<2, true><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, partial);
+  return cudaGetLastError();
+}
+}  // namespace ss

@@ -1,0 +1,467 @@
+// eri_kernel.cuh -- templates of the analytic ERI kernel (instantiated per class in eri_k*.cu).
+#pragma once
+//
+// Replaces gauss_ijkl (src/gauss_ijkl.F90:51-154) and its callees
+// bielec_integral / give_explicit_poly_and_gaussian / general_primitive_integral /
+// give_polynom_mult_center_x / I_x1_pol_mult* / I_x2_pol_mult / rint_sum.
+//
+// Design (GB300 FP64 is ~1/64 of the FP32 rate, so FP64 instruction count is the roofline):
+//  * primitive pairs are precomputed once per function pair (Gaussian product, K_AB screening
+//    of src/gaussian_product.F90:25-28 and src/give_explicit_poly_and_gaussian.F90:46-49; a
+//    screened pair contributes exactly 0 in the reference and is simply not stored);
+//  * one CTA per (function quartet, slice of bra primitive pairs); the ket primitive pairs of
+//    the quartet are staged in shared memory and read as broadcasts;
+//  * per primitive quartet the Boys values F_n(T) and the recursion coefficients are computed
+//    once and shared by all cartesian components of the r^2-type fits (the reference recomputes
+//    them for each of the up to 81 component combinations);
+//  * the recursive polynomial routines I_x1_pol_mult / I_x2_pol_mult become a bottom-up table
+//    I(a,c)(u), u = t^2, per axis, with the same per-coefficient operation order:
+//      I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1)
+//      I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
+//  * the thresholds of general_primitive_integral (|P_new| and |P_new Q_new| vs 1e-15,
+//    src/general_primitive_integral.F90:71,75,96,100,122,126) are applied at the same places;
+//  * partial sums go to a scratch buffer [quartet][slice] reduced in a fixed order, so results
+//    are run-to-run deterministic.
+#include <math.h>
+
+#include "ss_common.cuh"
+
+namespace ss {
+
+constexpr double THRESH = 1.e-15;
+constexpr double PI_5_2 = 34.9868366552;  // src/general_primitive_integral.F90:25
+
+// (x - x_A)^a around x_P: coefficients of (x-x_P)^i, pw1 = x_P - x_A
+// (src/give_explicit_poly_and_gaussian.F90:86-220, cases 0..4; the powers and the exact
+// integer binomials of each case)
+template <int L>
+__device__ __forceinline__ void recentered(double pw1, int a, double (&P)[L + 1]) {
+#pragma unroll
+  for (int t = 0; t <= L; t++) P[t] = 0.0;
+  if (a == 0) {
+    P[0] = 1.0;
+  } else if (a == 1) {
+    P[0] = pw1;
+    if (L >= 1) P[1 % (L + 1)] = 1.0;
+  } else if (a == 2) {
+    const double p2 = pw1 * pw1;
+    P[0] = p2;
+    if (L >= 2) { P[1 % (L + 1)] = 2.0 * pw1; P[2 % (L + 1)] = 1.0; }
+  } else if (a == 3) {
+    const double p2 = pw1 * pw1, p3 = p2 * pw1;
+    P[0] = p3;
+    if (L >= 3) { P[1 % (L + 1)] = 3.0 * p2; P[2 % (L + 1)] = 3.0 * pw1; P[3 % (L + 1)] = 1.0; }
+  } else {  // a == 4
+    const double p2 = pw1 * pw1, p3 = p2 * pw1, p4 = p2 * p2;
+    P[0] = p4;
+    if (L >= 4) {
+      P[1 % (L + 1)] = 4.0 * p3; P[2 % (L + 1)] = 6.0 * p2; P[3 % (L + 1)] = 4.0 * pw1;
+      P[4 % (L + 1)] = 1.0;
+    }
+  }
+}
+
+// P_new = recentered(A,a) * recentered(B,b) in multiply_poly's order (src/multiply_poly.F90:22-31)
+template <int L>
+__device__ __forceinline__ void pair_poly(double pa, int a, double pb, int b, double* Pn) {
+  double Pa[L + 1], Pb[L + 1];
+  recentered<L>(pa, a, Pa);
+  recentered<L>(pb, b, Pb);
+#pragma unroll
+  for (int t = 0; t <= L; t++) Pn[t] = 0.0;
+#pragma unroll
+  for (int ib = 0; ib <= L; ib++)
+#pragma unroll
+    for (int ic = 0; ic <= L; ic++)
+      if (ib + ic <= L && ib <= a && ic <= b) Pn[ib + ic] = Pn[ib + ic] + Pb[ic] * Pa[ib];
+}
+
+struct RecCoef {
+  double p10_1, p10_2, p01_1, p01_2, pq_inv;
+};
+
+// Bottom-up table I(a,c)[m] (coefficients of u = t^2) for a <= amax, c <= cmax (both <= L),
+// the same per-coefficient operation order as I_x1_pol_mult / I_x2_pol_mult:
+//   I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1);  I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
+template <int L>
+__device__ __forceinline__ void rys_table(const RecCoef& R, double Cc, double Dd, int amax, int cmax,
+                                          double (&I)[L + 1][L + 1][2 * L + 1]) {
+#pragma unroll
+  for (int c = 0; c <= L; c++) {
+    if (c > cmax) break;
+#pragma unroll
+    for (int m = 0; m <= 2 * L; m++) {
+      if (m > c) break;
+      double v = 0.0;
+      if (c == 0) {
+        v = 1.0;
+      } else {
+        if (c >= 2) {
+          if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (double)(c - 1));
+          if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (double)(c - 1));
+        }
+        if (m >= 1) v = v + Dd * I[0][c - 1][m - 1];
+      }
+      I[0][c][m] = v;
+    }
+  }
+#pragma unroll
+  for (int a = 1; a <= L; a++) {
+    if (a > amax) break;
+#pragma unroll
+    for (int c = 0; c <= L; c++) {
+      if (c > cmax) break;
+#pragma unroll
+      for (int m = 0; m <= 2 * L; m++) {
+        if (m > a + c) break;
+        double v = 0.0;
+        if (a >= 2) {
+          const double s = (double)(a - 1);
+          if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
+          if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
+        }
+        if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (double)c);
+        if (m >= 1) v = v + Cc * I[a - 1][c][m - 1];
+        I[a][c][m] = v;
+      }
+    }
+  }
+}
+
+// |x| < t and |x| > t on the bit patterns (integer pipe; x finite, t > 0)
+__device__ __forceinline__ bool abs_lt(double x, double t) {
+  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(t);
+}
+__device__ __forceinline__ bool abs_gt(double x, double t) {
+  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(t);
+}
+
+// Ix = sum_{ix,jx} (Pn[ix] Qn[jx]) I(ix,jx) with the thresholds of general_primitive_integral
+// (x axis: skip |P| < thresh; y, z: keep |P| > thresh; skip |P Q| < thresh).
+template <int L>
+__device__ __forceinline__ void axis_poly(const double* Pn, int degP, const double* Qn, int degQ,
+                                          const double (&I)[L + 1][L + 1][2 * L + 1], bool x_axis,
+                                          double* out) {
+#pragma unroll
+  for (int m = 0; m <= 2 * L; m++) out[m] = 0.0;
+#pragma unroll
+  for (int ix = 0; ix <= L; ix++) {
+    if (ix > degP) break;
+    const double a = Pn[ix];
+    if (x_axis ? abs_lt(a, THRESH) : !abs_gt(a, THRESH)) continue;
+#pragma unroll
+    for (int jx = 0; jx <= L; jx++) {
+      if (jx > degQ) break;
+      const double d = a * Qn[jx];
+      if (abs_lt(d, THRESH)) continue;
+#pragma unroll
+      for (int m = 0; m <= 2 * L; m++)
+        if (m <= ix + jx) out[m] = fma(d, I[ix][jx][m], out[m]);
+    }
+  }
+}
+
+static __constant__ double c_inv_odd[40] = {1.0 / 1.0, 1.0 / 3.0, 1.0 / 5.0, 1.0 / 7.0, 1.0 / 9.0, 1.0 / 11.0, 1.0 / 13.0, 1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0, 1.0 / 25.0, 1.0 / 27.0, 1.0 / 29.0, 1.0 / 31.0, 1.0 / 33.0, 1.0 / 35.0, 1.0 / 37.0, 1.0 / 39.0, 1.0 / 41.0, 1.0 / 43.0, 1.0 / 45.0, 1.0 / 47.0, 1.0 / 49.0, 1.0 / 51.0, 1.0 / 53.0, 1.0 / 55.0, 1.0 / 57.0, 1.0 / 59.0, 1.0 / 61.0, 1.0 / 63.0, 1.0 / 65.0, 1.0 / 67.0, 1.0 / 69.0, 1.0 / 71.0, 1.0 / 73.0, 1.0 / 75.0, 1.0 / 77.0, 1.0 / 79.0};  // 1/(2n+1)
+static __constant__ double c_inv_int[24] = {0.0, 1.0 / 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0, 1.0 / 9.0, 1.0 / 10.0, 1.0 / 11.0, 1.0 / 12.0, 1.0 / 13.0, 1.0 / 14.0, 1.0 / 15.0, 1.0 / 16.0, 1.0 / 17.0, 1.0 / 18.0, 1.0 / 19.0, 1.0 / 20.0, 1.0 / 21.0, 1.0 / 22.0, 1.0 / 23.0};  // 1/k (k >= 1)
+
+// Boys values F_0..F_nf(T) (nf <= NF).  T >= 1: the reference's erf + upward recursion
+// (src/rint_sum.F90:44-61), with erf(sqrt T) == 1 exactly for T > 36; T < 1: the Taylor series
+// of src/rint1.F90 for F_nf only, then the stable downward recursion
+// F_n = (2T F_{n+1} + e^-T)/(2n+1) (differs from the per-n Taylor sums by < 1e-15 relative).
+template <int NF>
+__device__ __forceinline__ void boys(double T, int nf, double (&F)[NF + 1]) {
+  const double sqpi = 1.7724538509055160273;  // dsqrt(dacos(-1.d0))
+  if (T < 1.0) {
+    if (T == 0.0) {
+#pragma unroll
+      for (int n = 0; n <= NF; n++) F[n] = c_inv_odd[n];
+      return;
+    }
+    double ck = 1.0, s = c_inv_odd[nf];
+#pragma unroll 1
+    for (int k = 1; k <= 22; k++) {
+      ck = ck * (-T) * c_inv_int[k];
+      const double term = ck * c_inv_odd[nf + k];
+      s = s + term;
+      if (abs_lt(term, 1.e-17)) break;
+    }
+    const double e = exp(-T);
+    F[NF] = 0.0;
+#pragma unroll
+    for (int n = NF; n >= 0; n--) {
+      if (n == nf) F[n] = s;
+      else if (n < nf) F[n] = fma(T + T, F[n + 1 <= NF ? n + 1 : NF], e) * c_inv_odd[n];
+    }
+  } else {
+    const double v = (T > 80.0) ? 0.0 : exp(-T);
+    const double u_inv = 1.0 / sqrt(T);
+    const double u = T * u_inv;
+    const double two_rho_inv = 0.5 * u_inv * u_inv;
+    const double val0 = 0.5 * u_inv * sqpi * (T > 36.0 ? 1.0 : erf(u));
+    F[0] = val0;
+    double rt = (val0 - v) * two_rho_inv;
+    double di = 3.0;
+#pragma unroll
+    for (int n = 1; n <= NF; n++) {
+      if (n > nf) break;
+      F[n] = rt;
+      rt = (rt * di - v) * two_rho_inv;
+      di = di + 2.0;
+    }
+  }
+}
+
+// Work per CTA: one function quartet (ik|jl) and a slice of its bra primitive pairs against all
+// its ket primitive pairs, the ket pairs staged in shared memory in tiles together with their
+// recentred polynomials.  Items (bra pair, ket pair) are dealt round-robin to the threads, so
+// every thread does the same number of primitive quartets.
+// T2: some of the four functions are r^2-type fits (3 cartesian components sharing exponents).
+template <int L, bool T2>
+__global__ void __launch_bounds__(128) eri_kernel(
+    BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
+    const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
+    const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
+    const int32_t* __restrict__ ls, double* __restrict__ partial) {
+  constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
+  constexpr int NF = (6 * L < 16) ? 6 * L : 16;
+  constexpr int QW = 3 * NO * (L + 1);  // ket polynomial doubles per ket pair
+  extern __shared__ double2 s_raw[];
+  PrimPair* s_ket = reinterpret_cast<PrimPair*>(s_raw);
+  double* s_q = reinterpret_cast<double*>(s_ket + ktile);
+  __shared__ double s_red[4];
+
+  const int64_t w = blockIdx.x / split;
+  const int part = blockIdx.x % split;
+  const int64_t q = work[w];
+  const int fi = is[q] - 1, fk = ks[q] - 1, fj = js[q] - 1, fl = ls[q] - 1;
+  const int64_t pb = ss_pair_index(fi, fk), pk = ss_pair_index(fj, fl);
+  const int nb = pair_cnt[pb], nk = pair_cnt[pk];
+  const PrimPair* bra = pp + pair_off[pb];
+  const PrimPair* ket = pp + pair_off[pk];
+
+  int np[4][3], t2[4];
+  const int fn[4] = {fi, fk, fj, fl};
+  int nf = 0;
+#pragma unroll
+  for (int f = 0; f < 4; f++) {
+    t2[f] = T2 ? (B.i_type[fn[f]] == 2) : 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      np[f][ax] = B.npower[3 * fn[f] + ax];
+      nf += np[f][ax];
+    }
+    nf += 2 * t2[f];
+  }
+  // per axis: powers of each option and maximal degrees
+  int amax[3], cmax[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++) {
+    amax[ax] = np[0][ax] + np[1][ax] + 2 * (t2[0] + t2[1]);
+    cmax[ax] = np[2][ax] + np[3][ax] + 2 * (t2[2] + t2[3]);
+  }
+
+  const int per = (nb + split - 1) / split;
+  const int b0 = part * per;
+  const int b1 = min(nb, b0 + per);
+  double acc = 0.0;
+
+  for (int t0 = 0; t0 < nk; t0 += ktile) {
+    const int kt = min(ktile, nk - t0);
+    __syncthreads();
+    {
+      const double2* src = reinterpret_cast<const double2*>(ket + t0);
+      for (int t = threadIdx.x; t < kt * 8; t += blockDim.x) s_raw[t] = src[t];
+    }
+    __syncthreads();
+    // recentred ket polynomials, per (ket pair, axis, option)
+    for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) {
+      const PrimPair& Q = s_ket[kk];
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++)
+#pragma unroll
+        for (int o = 0; o < NO; o++) {
+          if ((o & 1) && !t2[2]) continue;
+          if ((o & 2) && !t2[3]) continue;
+          pair_poly<L>(Q.PA[ax], np[2][ax] + 2 * (o & 1), Q.PB[ax], np[3][ax] + (o & 2),
+                       s_q + (size_t)kk * QW + (ax * NO + o) * (L + 1));
+        }
+    }
+    __syncthreads();
+
+    const int nitems = (b1 - b0) * kt;
+    int bcur = -1;
+    double Pn[3][NO][L + 1];
+    PrimPair P;
+    int ib = b0 + threadIdx.x / kt, ik = threadIdx.x % kt;  // item (bra, ket) of this thread
+    for (int e = threadIdx.x; e < nitems; e += blockDim.x) {
+      if (ib != bcur) {
+        P = bra[ib];
+        bcur = ib;
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++)
+#pragma unroll
+          for (int o = 0; o < NO; o++) {
+            if ((o & 1) && !t2[0]) continue;
+            if ((o & 2) && !t2[1]) continue;
+            pair_poly<L>(P.PA[ax], np[0][ax] + 2 * (o & 1), P.PB[ax], np[1][ax] + (o & 2), Pn[ax][o]);
+          }
+      }
+      const PrimPair& Q = s_ket[ik];
+      const double* Qn = s_q + (size_t)ik * QW;
+      const double p = P.p, qq = Q.p;
+      // src/general_primitive_integral.F90:54-60, 142-146
+      const double pq = P.p_inv * 0.5 * Q.p_inv;
+      const double pq_inv = 0.5 / (p + qq);
+      RecCoef R;
+      R.p10_1 = qq * pq;
+      R.p01_1 = p * pq;
+      const double pq_inv_2 = pq_inv + pq_inv;
+      R.p10_2 = pq_inv_2 * R.p10_1 * qq;
+      R.p01_2 = pq_inv_2 * R.p01_1 * p;
+      R.pq_inv = pq_inv;
+      const double rho = p * qq * pq_inv_2;
+      const double dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
+      const double T = (dx * dx + dy * dy + dz * dz) * rho;
+      double F[NF + 1];
+      boys<NF>(T, nf, F);
+
+      double accu;
+      if (!T2) {
+        double A[3][2 * L + 1];
+        int deg[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+          deg[ax] = amax[ax] + cmax[ax];
+          if (deg[ax] == 0) {
+            A[ax][0] = 1.0;
+#pragma unroll
+            for (int m = 1; m <= 2 * L; m++) A[ax][m] = 0.0;
+            continue;
+          }
+          double I[L + 1][L + 1][2 * L + 1];
+          const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
+          const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
+          rys_table<L>(R, Cc, Dd, amax[ax], cmax[ax], I);
+          axis_poly<L>(Pn[ax][0], amax[ax], Qn + ax * (L + 1), cmax[ax], I, ax == 0, A[ax]);
+        }
+        // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
+        double dp[4 * L + 1];
+#pragma unroll
+        for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
+#pragma unroll
+        for (int a = 0; a <= 2 * L; a++) {
+          if (a > deg[0]) break;
+#pragma unroll
+          for (int c = 0; c <= 2 * L; c++) {
+            if (c > deg[1]) break;
+            dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
+          }
+        }
+        double d1[NF + 1];
+#pragma unroll
+        for (int t = 0; t <= NF; t++) d1[t] = 0.0;
+#pragma unroll
+        for (int a = 0; a <= 4 * L; a++) {
+          if (a > deg[0] + deg[1] || a > NF) break;
+#pragma unroll
+          for (int c = 0; c <= 2 * L; c++) {
+            if (c > deg[2] || a + c > NF) break;
+            d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
+          }
+        }
+        accu = d1[0] * F[0];
+#pragma unroll
+        for (int n = 1; n <= NF; n++)
+          if (n <= nf) accu = fma(d1[n], F[n], accu);
+      } else {
+        // axis polynomials for every (bra option, ket option), then the cartesian combinations
+        double A[3][NO * NO][2 * L + 1];
+#pragma unroll 1
+        for (int ax = 0; ax < 3; ax++) {
+          double I[L + 1][L + 1][2 * L + 1];
+          const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
+          const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
+          rys_table<L>(R, Cc, Dd, amax[ax], cmax[ax], I);
+#pragma unroll 1
+          for (int ob = 0; ob < NO; ob++) {
+            if ((ob & 1) && !t2[0]) continue;
+            if ((ob & 2) && !t2[1]) continue;
+#pragma unroll 1
+            for (int oc = 0; oc < NO; oc++) {
+              if ((oc & 1) && !t2[2]) continue;
+              if ((oc & 2) && !t2[3]) continue;
+              const int da = np[0][ax] + np[1][ax] + 2 * (ob & 1) + (ob & 2);
+              const int dc = np[2][ax] + np[3][ax] + 2 * (oc & 1) + (oc & 2);
+              axis_poly<L>(Pn[ax][ob], da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0, A[ax][ob * NO + oc]);
+            }
+          }
+        }
+        accu = 0.0;
+        const int nci = t2[0] ? 3 : 1, nck = t2[1] ? 3 : 1, ncj = t2[2] ? 3 : 1, ncl = t2[3] ? 3 : 1;
+        for (int ci = 0; ci < nci; ci++)
+          for (int ck = 0; ck < nck; ck++)
+            for (int cj = 0; cj < ncj; cj++)
+              for (int cl = 0; cl < ncl; cl++) {
+                int sel[3], deg[3];
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                  const int ob = (t2[0] && ci == ax ? 1 : 0) | (t2[1] && ck == ax ? 2 : 0);
+                  const int oc = (t2[2] && cj == ax ? 1 : 0) | (t2[3] && cl == ax ? 2 : 0);
+                  sel[ax] = ob * NO + oc;
+                  deg[ax] = np[0][ax] + np[1][ax] + np[2][ax] + np[3][ax] + 2 * ((ob & 1) + (ob >> 1) + (oc & 1) + (oc >> 1));
+                }
+                const double* Ax = A[0][sel[0]];
+                const double* Ay = A[1][sel[1]];
+                const double* Az = A[2][sel[2]];
+                double dp[4 * L + 1];
+#pragma unroll
+                for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
+#pragma unroll
+                for (int a = 0; a <= 2 * L; a++) {
+                  if (a > deg[0]) break;
+#pragma unroll
+                  for (int c = 0; c <= 2 * L; c++) {
+                    if (c > deg[1]) break;
+                    dp[a + c] = fma(Ay[c], Ax[a], dp[a + c]);
+                  }
+                }
+                double d1[NF + 1];
+#pragma unroll
+                for (int t = 0; t <= NF; t++) d1[t] = 0.0;
+#pragma unroll
+                for (int a = 0; a <= 4 * L; a++) {
+                  if (a > deg[0] + deg[1] || a > NF) break;
+#pragma unroll
+                  for (int c = 0; c <= 2 * L; c++) {
+                    if (c > deg[2] || a + c > NF) break;
+                    d1[a + c] = fma(Az[c], dp[a], d1[a + c]);
+                  }
+                }
+                double s = d1[0] * F[0];
+#pragma unroll
+                for (int n = 1; n <= NF; n++)
+                  if (n <= nf) s = fma(d1[n], F[n], s);
+                accu = accu + s;
+              }
+      }
+      // src/general_primitive_integral.F90:192 and the coefficient product of src/gauss_ijkl.F90:137
+      const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv / sqrt(p + qq);
+      acc = fma(P.coef * Q.coef, pref * accu, acc);
+      // next item of this thread
+      ik += blockDim.x;
+      while (ik >= kt) {
+        ik -= kt;
+        ib++;
+      }
+    }
+  }
+  // block reduction in a fixed order
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) partial[w * split + part] = ((s_red[0] + s_red[1]) + s_red[2]) + s_red[3];
+}
+
+
+}  // namespace ss

@@ -13,9 +13,10 @@
 #include "ss_context.cuh"
 
 namespace ss {
-size_t eri_smem_bytes(int max_cnt);
-cudaError_t launch_eri_class(int L, dim3 grid, size_t smem, cudaStream_t st, const BasisDev& B,
-                             const PrimPair* pp, const int64_t* off, const int* cnt,
+cudaError_t eri_init_constants();
+void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem);
+cudaError_t launch_eri_class(int L, bool t2, dim3 grid, int ktile, size_t smem, cudaStream_t st,
+                             const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, double* partial);
 __global__ void prim_pair_count(BasisDev B, int npairs, int* cnt);
@@ -121,12 +122,14 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const int32_t* d_qls, const std::vector<int32_t>& qis, const std::vector<int32_t>& qjs,
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out) {
-  // bucket by class L = max(bra L, ket L)
-  std::vector<std::vector<int64_t>> bucket(SS_MAX_POW + 1);
+  // bucket by class (L = max(bra L, ket L), any r^2-type fit among the four functions)
+  const int NB = 2 * (SS_MAX_POW + 1);
+  std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
     int i = qis[t] - 1, k = qks[t] - 1, j = qjs[t] - 1, l = qls[t] - 1;
     int L = std::max(pair_L(c, i, k), pair_L(c, j, l));
-    bucket[L].push_back(t);
+    bool t2 = c->h_itype[i] == 2 || c->h_itype[k] == 2 || c->h_itype[j] == 2 || c->h_itype[l] == 2;
+    bucket[2 * L + (t2 ? 1 : 0)].push_back(t);
   }
   int64_t nsel = (int64_t)sel.size();
   // one split for all classes keeps the slot arithmetic simple
@@ -136,18 +139,18 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   split_out = split;
   std::vector<int64_t> work;
   work.reserve(nsel);
-  std::vector<int64_t> begin(SS_MAX_POW + 1), count(SS_MAX_POW + 1);
-  std::vector<int> maxk(SS_MAX_POW + 1, 0);
+  std::vector<int64_t> begin(NB), count(NB);
+  std::vector<int> maxk(NB, 0);
   slot_of_sel.assign(qis.size(), -1);
-  for (int L = 0; L <= SS_MAX_POW; L++) {
-    begin[L] = (int64_t)work.size();
-    for (int64_t t : bucket[L]) {
+  for (int bk = 0; bk < NB; bk++) {
+    begin[bk] = (int64_t)work.size();
+    for (int64_t t : bucket[bk]) {
       slot_of_sel[t] = (int64_t)work.size();
       work.push_back(t);
       int j = qjs[t] - 1, l = qls[t] - 1;
-      maxk[L] = std::max(maxk[L], c->h_pp_cnt[ss_pair_index(j, l)]);
+      maxk[bk] = std::max(maxk[bk], c->h_pp_cnt[ss_pair_index(j, l)]);
     }
-    count[L] = (int64_t)work.size() - begin[L];
+    count[bk] = (int64_t)work.size() - begin[bk];
   }
   int rc = h2d(c, c->d_scratch_a, work.data(), sizeof(int64_t) * std::max<size_t>(work.size(), 1));
   if (rc) return rc;
@@ -155,18 +158,22 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   if (rc) return rc;
   const int64_t* d_work = (const int64_t*)c->d_scratch_a.ptr;
   double* d_partial = (double*)c->d_scratch_b.ptr;
-  for (int L = 0; L <= SS_MAX_POW; L++) {
-    if (!count[L]) continue;
-    size_t smem = eri_smem_bytes(std::max(maxk[L], 1));
+  for (int bk = 0; bk < NB; bk++) {
+    if (!count[bk]) continue;
+    const int L = bk / 2;
+    const bool t2 = bk & 1;
+    int ktile;
+    size_t smem;
+    eri_tile(L, t2, std::max(maxk[bk], 1), &ktile, &smem);
     // grid.x is limited to 2^31-1: launch in chunks of quartets
     const int64_t chunk = (int64_t)(2147483647 / split);
-    for (int64_t s0 = 0; s0 < count[L]; s0 += chunk) {
-      int64_t nq = std::min(chunk, count[L] - s0);
+    for (int64_t s0 = 0; s0 < count[bk]; s0 += chunk) {
+      int64_t nq = std::min(chunk, count[bk] - s0);
       dim3 grid((unsigned)(nq * split));
-      cudaError_t e = launch_eri_class(L, grid, smem, c->stream, c->basis, (const PrimPair*)c->d_pp.ptr,
-                                       (const int64_t*)c->d_pp_off.ptr, (const int*)c->d_pp_cnt.ptr,
-                                       d_work + begin[L] + s0, split, d_qis, d_qjs, d_qks, d_qls,
-                                       d_partial + (begin[L] + s0) * split);
+      cudaError_t e = launch_eri_class(L, t2, grid, ktile, smem, c->stream, c->basis,
+                                       (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
+                                       (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
+                                       d_qjs, d_qks, d_qls, d_partial + (begin[bk] + s0) * split);
       if (e != cudaSuccess) {
         ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
         return SS_ERR_CUDA;
@@ -420,6 +427,7 @@ int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower,
   int npairs = nbasis * (nbasis + 1) / 2;
   rc = dev_alloc(c, c->d_pp_cnt, sizeof(int) * npairs);
   if (rc) return rc;
+  SS_CUDA_TRY(eri_init_constants());
   prim_pair_count<<<npairs, 128, 0, c->stream>>>(c->basis, npairs, (int*)c->d_pp_cnt.ptr);
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;

@@ -3,18 +3,18 @@
 * primitive quartets: the reference loops over n_gauss(i)*nc(i) x ... x n_gauss(l)*nc(l)
   primitive Gaussian products per (ik|jl) (src/gauss_ijkl.F90:127-150), nc = 3 for the
   r^2-type fits (i_type 2) and 1 otherwise.
-* FP64 flops per primitive quartet of the analytic kernel, per angular class L (the largest
-  per-axis power of a bra or ket pair, incl. the +2 of r^2 fits): FP64 instructions executed
-  by eri_kernel<L> (DFMA counted as 2 flops, DMUL/DADD as 1) divided by the primitive quartets
-  of the launch, from an ncu capture; the table and the capture command are recorded in
-  profiles/eri_kernel_h2o26.md.
+* FP64 flops per primitive quartet of the analytic stage (all eri_kernel launches of one
+  job, Schwarz diagonal included): FP64 instructions executed (DFMA counted as 2 flops,
+  DMUL/DADD as 1) divided by the primitive quartets, from an ncu capture of the H2O
+  26-function basis with 6-Gaussian fits (same kernels and angular classes as the 20-Gaussian
+  workload).  The capture command and per-class table are in profiles/eri_kernel_h2o26.md.
 """
 from __future__ import annotations
 
 import numpy as np
 
-# eri_kernel<L>: executed FP64 flops per primitive quartet (ncu); None = not yet measured
-FLOPS_PER_PRIM_BY_L = {0: None, 1: None, 2: None, 3: None, 4: None}
+# executed FP64 flops per primitive quartet of the analytic stage (ncu, see module doc)
+EXEC_FLOPS_PER_PRIM = 241.5
 
 
 def _pair_L(b, f1, f2):
@@ -41,12 +41,6 @@ def primitive_quartets(b, quartets) -> float:
     return float(sum(primitive_quartets_by_class(b, quartets).values()))
 
 
-def eri_fp64_flops(b, quartets):
-    """Executed FP64 flops of the analytic stage (None if a class is unmeasured)."""
-    tot = 0.0
-    for L, n in primitive_quartets_by_class(b, quartets).items():
-        f = FLOPS_PER_PRIM_BY_L.get(L)
-        if f is None:
-            return None
-        tot += f * n
-    return tot
+def eri_fp64_flops(b, quartets) -> float:
+    """Executed FP64 flops of the analytic stage of one job."""
+    return EXEC_FLOPS_PER_PRIM * primitive_quartets(b, quartets)
