@@ -143,6 +143,12 @@ int ss_split_bf16_gemm_noalloc(void* stream, int P, int64_t K, const uint16_t* a
 int ss_psd_clean(ss_ctx* ctx, double* moy, int layout, int rank, int oversample, int q,
                  uint64_t seed, int* n_removed);
 
+/* Exact removal of the negative eigencomponents of the ERI matrix in `layout` (replaces the
+ * nbasis < 200 path of davidson_clean, src/davidson_clean.F90:30-116): full FP64
+ * eigen-decomposition on the device, W -= sum_{lambda<0} lambda v v^T, canonical entries read
+ * back into moy.  Matrix dimension <= 1024.  n_removed receives the removed count. */
+int ss_psd_project(ss_ctx* ctx, double* moy, int layout, int* n_removed);
+
 /* Lowest m eigenpairs of the ERI matrix in `layout` by Davidson with FP64 Rayleigh-Ritz
  * (follows src/davidson.F90:1-158).  evals (m), evecs (N x m column-major) may be NULL. */
 int ss_davidson(ss_ctx* ctx, const double* moy, int layout, int m, double tol, int max_iter,

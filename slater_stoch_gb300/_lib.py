@@ -53,6 +53,7 @@ SIGNATURES = {
                                C.c_void_p]),
     "ss_davidson": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
                               C.c_void_p]),
+    "ss_psd_project": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_void_p]),
 }
 
 

@@ -174,6 +174,13 @@ class Context:
                                         int(q), int(seed), _ptr(nrem)))
         return moy, int(nrem[0])
 
+    def psd_project(self, moy, layout: str = "packed_pair"):
+        """Exact removal of negative eigencomponents (davidson_clean's small-basis path)."""
+        moy = np.array(moy, dtype=np.float64, copy=True)
+        nrem = np.zeros(1, np.int32)
+        _lib.check(self._L.ss_psd_project(self._h, moy, LAYOUTS[layout], _ptr(nrem)))
+        return moy, int(nrem[0])
+
     def davidson(self, moy, m: int = 10, layout: str = "packed_pair", tol: float = 1e-8,
                  max_iter: int = 200):
         moy = np.ascontiguousarray(moy, np.float64)

@@ -1,13 +1,653 @@
-// cleanup.cu -- PSD cleanup and Davidson entry points (kernels land with the cleanup stage).
+// cleanup.cu -- PSD cleanup of the ERI matrix (svd_clean) and Davidson, FP64 on the device.
+//
+// ss_psd_clean restates src/svd_clean.F90:1-426 for one GPU: the ERIs are scattered into the
+// symmetric matrix W (the reference's n^2 x n^2 <ij|kl> arrangement, or the packed Coulomb
+// metric M[(ik),(jl)] = (ik|jl)); passes of a randomized SVD (Gaussian test matrix, q power
+// iterations with Householder re-orthogonalisation, SVD of Y = Z^T W_work) find components
+// U D V^T; the sign test <U_k, V_k> gives the eigenvalue sign and drops unresolved components;
+// all found components are deflated from W_work and the negative ones are removed from W; the
+// loop ends when npass >= N or max|D| < 1e-12; the cleaned ERIs are gathered back.  The SVD
+// of Y comes from the eigen-decomposition of Y Y^T (Y Y^T = UY D^2 UY^T, V^T = D^-1 UY^T Y);
+// components it cannot resolve relative to the largest one fail the sign test and are found
+// in later passes, after the deflation has removed the large ones.
+//
+// ss_davidson restates src/davidson.F90:1-158 (lowest m eigenpairs, NMAX = min(10, N/m),
+// diagonal preconditioner (E u - H u)/max(H_ii - E, 1e-2), convergence when the largest
+// correction norm is < tol); the basis is kept orthonormal so the projected problem is a
+// standard symmetric eigenproblem (the reference solves the equivalent generalized one with
+// dsygv).
+#include <cublas_v2.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "linalg.cuh"
+#include "philox.cuh"
 #include "ss_common.cuh"
 #include "ss_context.cuh"
+
+namespace ss {
+
+#define TRY(x)           \
+  do {                   \
+    int _rc = (x);       \
+    if (_rc) return _rc; \
+  } while (0)
+#define CUBLAS_TRY(x)                                                       \
+  do {                                                                      \
+    cublasStatus_t _s = (x);                                                \
+    if (_s != CUBLAS_STATUS_SUCCESS) {                                      \
+      ss_set_error_msg("cuBLAS error %d at %s:%d", (int)_s, __FILE__, __LINE__); \
+      return SS_ERR_CUDA;                                                   \
+    }                                                                       \
+  } while (0)
+
+static int get_cublas(ss_ctx* c, cublasHandle_t* h) {
+  if (!c->cublas_handle) {
+    cublasHandle_t hh;
+    CUBLAS_TRY(cublasCreate(&hh));
+    CUBLAS_TRY(cublasSetStream(hh, c->stream));
+    c->cublas_handle = (void*)hh;
+  }
+  *h = (cublasHandle_t)c->cublas_handle;
+  return SS_OK;
+}
+
+void destroy_cublas(void* h) {
+  if (h) cublasDestroy((cublasHandle_t)h);
+}
+
+// ---------------------------------------------------------------------------------------
+// scatter / gather between the quartet list and the symmetric matrix
+// ---------------------------------------------------------------------------------------
+// REF_N2: W(ii,jj), ii = i + j n, jj = k + l n (0-based), the 8 permutations of
+// src/svd_clean.F90:97-130; PACKED_PAIR: M(p(ik), p(jl)) and its transpose.
+__device__ __forceinline__ void perm8(int t, int i, int j, int k, int l, int& a, int& b, int& c, int& d) {
+  switch (t) {
+    case 0: a = i; b = j; c = k; d = l; break;
+    case 1: a = k; b = j; c = i; d = l; break;
+    case 2: a = k; b = l; c = i; d = j; break;
+    case 3: a = i; b = l; c = k; d = j; break;
+    case 4: a = j; b = i; c = l; d = k; break;
+    case 5: a = j; b = k; c = l; d = i; break;
+    case 6: a = l; b = k; c = j; d = i; break;
+    default: a = l; b = i; c = j; d = k; break;
+  }
+}
+
+__global__ void scatter_kernel(int64_t nint, int layout, int n, int64_t N, const int32_t* __restrict__ is,
+                               const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
+                               const int32_t* __restrict__ ls, const double* __restrict__ moy,
+                               double* __restrict__ W) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int i = is[q] - 1, j = js[q] - 1, k = ks[q] - 1, l = ls[q] - 1;
+  const double v = moy[q];
+  if (layout == SS_LAYOUT_REF_N2) {
+    for (int t = 0; t < 8; t++) {
+      int a, b, c, d;
+      perm8(t, i, j, k, l, a, b, c, d);
+      const int64_t ii = a + (int64_t)b * n, jj = c + (int64_t)d * n;
+      W[ii + jj * N] = v;  // column-major
+    }
+  } else {
+    const int64_t p1 = ss_pair_index(i, k), p2 = ss_pair_index(j, l);
+    W[p1 + p2 * N] = v;
+    W[p2 + p1 * N] = v;
+  }
+}
+
+__global__ void gather_kernel(int64_t nint, int layout, int n, int64_t N, const int32_t* __restrict__ is,
+                              const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
+                              const int32_t* __restrict__ ls, const double* __restrict__ W,
+                              double* __restrict__ moy) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int i = is[q] - 1, j = js[q] - 1, k = ks[q] - 1, l = ls[q] - 1;
+  double v = 0.0;
+  if (layout == SS_LAYOUT_REF_N2) {  // src/svd_clean.F90:372-405
+    for (int t = 0; t < 8; t++) {
+      int a, b, c, d;
+      perm8(t, i, j, k, l, a, b, c, d);
+      const int64_t ii = a + (int64_t)b * n, jj = c + (int64_t)d * n;
+      v = v + W[ii + jj * N] * 0.125;
+    }
+  } else {
+    const int64_t p1 = ss_pair_index(i, k), p2 = ss_pair_index(j, l);
+    v = 0.5 * (W[p1 + p2 * N] + W[p2 + p1 * N]);
+  }
+  moy[q] = v;
+}
+
+// Gaussian test matrix (src/svd_clean.F90:159-171): Box-Muller from Philox, columns normalised
+__global__ void gaussian_matrix_kernel(uint64_t seed, uint32_t pass, int N, int r, double* __restrict__ P) {
+  const int k = blockIdx.x;
+  __shared__ double sh[32];
+  double ss = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const uint64_t idx = (uint64_t)k * N + i;
+    uint32_t c[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), pass, STREAM_SVD};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u1 = u01_open(c[0], c[1]), u2 = u01_open(c[2], c[3]);
+    const double v = sqrt(-2.0 * log(u1)) * cos(6.283185307179586477 * u2);
+    P[(size_t)k * N + i] = v;
+    ss += v * v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    sh[0] = 1.0 / sqrt(t);
+  }
+  __syncthreads();
+  const double inv = sh[0];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) P[(size_t)k * N + i] *= inv;
+}
+
+// r_k = <U_k, Vt_k>; U (N x r col-major), Vt (r x N col-major, ld r)
+__global__ void sign_test_kernel(int N, int r, const double* __restrict__ U, const double* __restrict__ Vt,
+                                 double* __restrict__ rk) {
+  const int k = blockIdx.x;
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) s += U[(size_t)k * N + i] * Vt[k + (size_t)i * r];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    rk[k] = t;
+  }
+}
+
+// columns of U scaled: out(:,k) = U(:,k) * s[k]
+__global__ void scale_cols_kernel(int N, int r, const double* __restrict__ U, const double* __restrict__ s,
+                                  double* __restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)N * r) return;
+  out[e] = U[e] * s[e / N];
+}
+
+// Vt rows scaled by inv[k] (r x N col-major, ld r)
+__global__ void scale_rows_kernel(int r, int N, double* __restrict__ Vt, const double* __restrict__ inv) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)N * r) return;
+  Vt[e] *= inv[e % r];
+}
+
+// reverse column order of a (n x n row-major eigenvectors) into out col-major (largest first)
+__global__ void reverse_eigvec_kernel(int n, const double* __restrict__ a, double* __restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * n) return;
+  const int row = (int)(e % n), col = (int)(e / n);  // out col-major (row, col)
+  out[e] = a[(size_t)row * n + (n - 1 - col)];
+}
+
+__global__ void transpose_sym_kernel(int n, const double* __restrict__ in, double* __restrict__ out) {
+  // out row-major = symmetrised in (col-major)
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * n) return;
+  const int i = (int)(e / n), j = (int)(e % n);
+  out[e] = 0.5 * (in[i + (size_t)j * n] + in[j + (size_t)i * n]);
+}
+
+static unsigned nb(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+int psd_clean(ss_ctx* c, double* moy_host, int layout, int rank, int oversample, int q, uint64_t seed,
+              int* n_removed) {
+  const int n = c->n;
+  const int64_t N64 = layout == SS_LAYOUT_REF_N2 ? (int64_t)n * n : (int64_t)n * (n + 1) / 2;
+  if (N64 > 16384) {
+    ss_set_error_msg("psd_clean: matrix dimension %lld too large for the dense device cleanup", (long long)N64);
+    return SS_ERR_UNSUPPORTED;
+  }
+  const int N = (int)N64;
+  const int r = std::min(rank + oversample, N);
+  if (r < 1 || r > 1024) {
+    ss_set_error_msg("psd_clean: rank + oversample must be in 1..1024 (got %d)", r);
+    return SS_ERR_ARG;
+  }
+  cublasHandle_t hb;
+  TRY(get_cublas(c, &hb));
+  void* p;
+  double *W, *Ww, *P, *Z, *Qw, *tau, *Y, *G, *ev, *ework, *UY, *U, *Vt, *Us, *Dd, *rk, *moy;
+  int* info;
+  const size_t NN = (size_t)N * N, Nr = (size_t)N * r, rr = (size_t)r * r;
+  TRY(pool_get(c, "cl_W", sizeof(double) * NN, &p)); W = (double*)p;
+  TRY(pool_get(c, "cl_Ww", sizeof(double) * NN, &p)); Ww = (double*)p;
+  TRY(pool_get(c, "cl_P", sizeof(double) * Nr, &p)); P = (double*)p;
+  TRY(pool_get(c, "cl_Z", sizeof(double) * Nr, &p)); Z = (double*)p;
+  TRY(pool_get(c, "cl_Qw", sizeof(double) * Nr, &p)); Qw = (double*)p;
+  TRY(pool_get(c, "cl_tau", sizeof(double) * r, &p)); tau = (double*)p;
+  TRY(pool_get(c, "cl_Y", sizeof(double) * Nr, &p)); Y = (double*)p;
+  TRY(pool_get(c, "cl_G", sizeof(double) * rr, &p)); G = (double*)p;
+  TRY(pool_get(c, "cl_ev", sizeof(double) * r, &p)); ev = (double*)p;
+  TRY(pool_get(c, "cl_ework", sizeof(double) * 2 * r, &p)); ework = (double*)p;
+  TRY(pool_get(c, "cl_UY", sizeof(double) * rr, &p)); UY = (double*)p;
+  TRY(pool_get(c, "cl_U", sizeof(double) * Nr, &p)); U = (double*)p;
+  TRY(pool_get(c, "cl_Vt", sizeof(double) * Nr, &p)); Vt = (double*)p;
+  TRY(pool_get(c, "cl_Us", sizeof(double) * Nr, &p)); Us = (double*)p;
+  TRY(pool_get(c, "cl_D", sizeof(double) * r, &p)); Dd = (double*)p;
+  TRY(pool_get(c, "cl_rk", sizeof(double) * r, &p)); rk = (double*)p;
+  TRY(pool_get(c, "cl_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
+  TRY(pool_get(c, "cl_info", sizeof(int), &p)); info = (int*)p;
+  cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
+  SS_CUDA_TRY(cudaMemsetAsync(Ww, 0, sizeof(double) * NN, st));
+  scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
+                                               (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+                                               (const int32_t*)c->d_ls.ptr, moy, Ww);
+  SS_CUDA_TRY(cudaGetLastError());
+  SS_CUDA_TRY(cudaMemcpyAsync(W, Ww, sizeof(double) * NN, cudaMemcpyDeviceToDevice, st));
+  c->launches++;
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  int npass = 0, removed = 0;
+  uint32_t pass = 0;
+  std::vector<double> hD(r), hR(r), hev(r);
+  while (npass < N) {
+    gaussian_matrix_kernel<<<r, 256, 0, st>>>(seed, pass, N, r, P);
+    SS_CUDA_TRY(cudaGetLastError());
+    // Z = W_work P; orthonormalise
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, N, &one, Ww, N, P, N, &zero, Z, N));
+    TRY(ortho_qr(st, N, r, Z, N, Qw, tau, &c->launches));
+    for (int it = 0; it < q; it++) {  // power iterations (src/svd_clean.F90:212-255)
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, N, r, N, &one, Ww, N, Z, N, &zero, P, N));
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, N, &one, Ww, N, P, N, &zero, Z, N));
+      TRY(ortho_qr(st, N, r, Z, N, Qw, tau, &c->launches));
+    }
+    // Y = Z^T W_work (r x N, ld r); Y Y^T = UY D^2 UY^T
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, r, N, N, &one, Z, N, Ww, N, &zero, Y, r));
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, r, r, N, &one, Y, r, Y, r, &zero, G, r));
+    transpose_sym_kernel<<<nb((int64_t)r * r), 256, 0, st>>>(r, G, UY);  // UY (row-major) = sym(G)
+    TRY(sym_eig(st, r, UY, ev, ework, info, &c->launches));
+    reverse_eigvec_kernel<<<nb((int64_t)r * r), 256, 0, st>>>(r, UY, G);  // G <- UY col-major, descending
+    c->launches += 5;
+    SS_CUDA_TRY(cudaMemcpyAsync(hev.data(), ev, sizeof(double) * r, cudaMemcpyDeviceToHost, st));
+    int hinfo = 0;
+    SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SS_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hinfo) {
+      ss_set_error_msg("psd_clean: symmetric eigensolver did not converge (%d)", hinfo);
+      return SS_ERR_NUMERIC;
+    }
+    std::vector<double> inv(r);
+    for (int k = 0; k < r; k++) {
+      hD[k] = sqrt(std::max(hev[r - 1 - k], 0.0));
+      inv[k] = hD[k] > 0.0 ? 1.0 / hD[k] : 0.0;
+    }
+    SS_CUDA_TRY(cudaMemcpyAsync(Dd, inv.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
+    // Vt = D^-1 UY^T Y ; U = Z UY
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, r, N, r, &one, G, r, Y, r, &zero, Vt, r));
+    scale_rows_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(r, N, Vt, Dd);
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, r, &one, Z, N, G, r, &zero, U, N));
+    sign_test_kernel<<<r, 256, 0, st>>>(N, r, U, Vt, rk);
+    c->launches += 2;
+    SS_CUDA_TRY(cudaMemcpyAsync(hR.data(), rk, sizeof(double) * r, cudaMemcpyDeviceToHost, st));
+    SS_CUDA_TRY(cudaStreamSynchronize(st));
+    // sign test (src/svd_clean.F90:286-296)
+    npass += r;
+    double dmax = 0.0;
+    std::vector<double> absD(r), negD(r);
+    int nneg = 0;
+    for (int k = 0; k < r; k++) {
+      if (hR[k] < 0.0) hD[k] = -hD[k];
+      if (fabs(hR[k]) < 0.99) {
+        hD[k] = 0.0;
+        npass--;
+      }
+      absD[k] = fabs(hD[k]);
+      negD[k] = hD[k] < 0.0 ? hD[k] : 0.0;
+      if (hD[k] < 0.0) nneg++;
+      dmax = std::max(dmax, fabs(hD[k]));
+    }
+    // W_work -= U |D| Vt ; W += U D_neg Vt   (src/svd_clean.F90:335-353)
+    SS_CUDA_TRY(cudaMemcpyAsync(Dd, absD.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
+    scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, Dd, Us);
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, N, r, &mone, Us, N, Vt, r, &one, Ww, N));
+    if (nneg) {
+      SS_CUDA_TRY(cudaMemcpyAsync(Dd, negD.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
+      scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, Dd, Us);
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, N, r, &one, Us, N, Vt, r, &one, W, N));
+      c->launches++;
+      removed += nneg;
+    }
+    c->launches++;
+    if (dmax < 1.e-12) npass = N;  // src/svd_clean.F90:359
+    pass++;
+    if (pass > 1000) {
+      ss_set_error_msg("psd_clean: no convergence after 1000 passes");
+      return SS_ERR_NUMERIC;
+    }
+  }
+  gather_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
+                                              (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+                                              (const int32_t*)c->d_ls.ptr, W, moy);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (n_removed) *n_removed = removed;
+  return SS_OK;
+}
+
+// canonical read-back of src/davidson_clean.F90:108-112 (moy = W(ii,jj), no averaging)
+__global__ void gather_canonical_kernel(int64_t nint, int layout, int n, int64_t N, const int32_t* __restrict__ is,
+                                        const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
+                                        const int32_t* __restrict__ ls, const double* __restrict__ W,
+                                        double* __restrict__ moy) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int i = is[q] - 1, j = js[q] - 1, k = ks[q] - 1, l = ls[q] - 1;
+  if (layout == SS_LAYOUT_REF_N2)
+    moy[q] = W[(i + (int64_t)j * n) + (k + (int64_t)l * n) * N];
+  else
+    moy[q] = W[ss_pair_index(i, k) + ss_pair_index(j, l) * N];
+}
+
+__global__ void copy_rowmajor_kernel(int64_t NN, const double* __restrict__ in, double* __restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e < NN) out[e] = in[e];  // W is symmetric: column-major == row-major
+}
+
+// V (row-major eigenvectors, N x N) columns 0..nneg-1 scaled by the eigenvalues -> Vs col-major,
+// Vc col-major copy (for W -= Vs Vc^T)
+__global__ void neg_components_kernel(int N, int nneg, const double* __restrict__ V, const double* __restrict__ ev,
+                                      double* __restrict__ Vs, double* __restrict__ Vc) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)N * nneg) return;
+  const int row = (int)(e % N), col = (int)(e / N);
+  const double v = V[(size_t)row * N + col];
+  Vc[e] = v;
+  Vs[e] = v * ev[col];
+}
+
+// Remove the negative eigencomponents exactly (src/davidson_clean.F90:30-116, the path the
+// reference takes for nbasis < 200): full FP64 eigen-decomposition of the ERI matrix, then
+// W -= sum_{lambda_k < 0} lambda_k v_k v_k^T and the canonical entries are read back.  With the
+// packed Coulomb metric the result is exactly PSD (to rounding, ~1e-15 of the largest eigenvalue).
+int psd_project(ss_ctx* c, double* moy_host, int layout, int* n_removed) {
+  const int n = c->n;
+  const int64_t N64 = layout == SS_LAYOUT_REF_N2 ? (int64_t)n * n : (int64_t)n * (n + 1) / 2;
+  if (N64 > 1024) {
+    ss_set_error_msg("psd_project: matrix dimension %lld above the 1024 of the device eigensolver",
+                     (long long)N64);
+    return SS_ERR_UNSUPPORTED;
+  }
+  const int N = (int)N64;
+  cublasHandle_t hb;
+  TRY(get_cublas(c, &hb));
+  void* p;
+  double *W, *A, *ev, *ework, *Vs, *Vc, *moy;
+  int* info;
+  const size_t NN = (size_t)N * N;
+  TRY(pool_get(c, "pj_W", sizeof(double) * NN, &p)); W = (double*)p;
+  TRY(pool_get(c, "pj_A", sizeof(double) * NN, &p)); A = (double*)p;
+  TRY(pool_get(c, "pj_ev", sizeof(double) * N, &p)); ev = (double*)p;
+  TRY(pool_get(c, "pj_ework", sizeof(double) * 2 * N, &p)); ework = (double*)p;
+  TRY(pool_get(c, "pj_Vs", sizeof(double) * NN, &p)); Vs = (double*)p;
+  TRY(pool_get(c, "pj_Vc", sizeof(double) * NN, &p)); Vc = (double*)p;
+  TRY(pool_get(c, "pj_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
+  TRY(pool_get(c, "pj_info", sizeof(int), &p)); info = (int*)p;
+  cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
+  SS_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double) * NN, st));
+  scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
+                                               (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+                                               (const int32_t*)c->d_ls.ptr, moy, W);
+  copy_rowmajor_kernel<<<nb((int64_t)NN), 256, 0, st>>>((int64_t)NN, W, A);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches += 2;
+  TRY(sym_eig(st, N, A, ev, ework, info, &c->launches));
+  std::vector<double> hev(N);
+  int hinfo = 0;
+  SS_CUDA_TRY(cudaMemcpyAsync(hev.data(), ev, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hinfo) {
+    ss_set_error_msg("psd_project: symmetric eigensolver did not converge (%d)", hinfo);
+    return SS_ERR_NUMERIC;
+  }
+  int nneg = 0;
+  while (nneg < N && hev[nneg] < 0.0) nneg++;  // ascending order
+  if (nneg) {
+    neg_components_kernel<<<nb((int64_t)N * nneg), 256, 0, st>>>(N, nneg, A, ev, Vs, Vc);
+    const double mone = -1.0, one = 1.0;
+    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, N, N, nneg, &mone, Vs, N, Vc, N, &one, W, N));
+    c->launches += 2;
+  }
+  gather_canonical_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
+                                                        (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+                                                        (const int32_t*)c->d_ls.ptr, W, moy);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (n_removed) *n_removed = nneg;
+  return SS_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Davidson
+// ---------------------------------------------------------------------------------------
+__global__ void diag_kernel(int N, const double* __restrict__ H, double* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) d[i] = H[i + (size_t)i * N];
+}
+
+// correction vectors (src/davidson.F90:132-140): c_j = (E_j x_j - w_j)/max(H_ii - E_j, 1e-2)
+__global__ void davidson_correction(int N, int m, const double* __restrict__ X, const double* __restrict__ WX,
+                                    const double* __restrict__ E, const double* __restrict__ Hd,
+                                    double* __restrict__ Cout) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)N * m) return;
+  const int i = (int)(e % N), j = (int)(e / N);
+  Cout[e] = (E[j] * X[e] - WX[e]) / fmax(Hd[i] - E[j], 1.e-2);
+}
+
+__global__ void col_norms_kernel(int N, int m, const double* __restrict__ X, double* __restrict__ nrm) {
+  const int k = blockIdx.x;
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) s += X[(size_t)k * N + i] * X[(size_t)k * N + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    nrm[k] = sqrt(t);
+  }
+}
+
+int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, int max_iter, double* evals,
+             double* evecs) {
+  const int n = c->n;
+  const int64_t N64 = layout == SS_LAYOUT_REF_N2 ? (int64_t)n * n : (int64_t)n * (n + 1) / 2;
+  if (N64 > 16384 || m < 1 || m > N64) {
+    ss_set_error_msg("davidson: bad sizes (N=%lld, m=%d)", (long long)N64, m);
+    return SS_ERR_ARG;
+  }
+  const int N = (int)N64;
+  const int nmax = std::max(2, std::min(10, N / m));  // src/davidson.F90:21
+  const int kmax = nmax * m;
+  if (kmax > N) {
+    ss_set_error_msg("davidson: subspace %d larger than the matrix %d", kmax, N);
+    return SS_ERR_ARG;
+  }
+  cublasHandle_t hb;
+  TRY(get_cublas(c, &hb));
+  void* p;
+  double *H, *Hd, *U, *WU, *S, *Sa, *ev, *ework, *X, *WX, *Cc, *E, *nrm, *tmp, *moy, *Qw, *tau;
+  int* info;
+  const size_t NN = (size_t)N * N, Nk = (size_t)N * kmax;
+  TRY(pool_get(c, "dv_H", sizeof(double) * NN, &p)); H = (double*)p;
+  TRY(pool_get(c, "dv_Hd", sizeof(double) * N, &p)); Hd = (double*)p;
+  TRY(pool_get(c, "dv_U", sizeof(double) * Nk, &p)); U = (double*)p;
+  TRY(pool_get(c, "dv_WU", sizeof(double) * Nk, &p)); WU = (double*)p;
+  TRY(pool_get(c, "dv_S", sizeof(double) * kmax * kmax, &p)); S = (double*)p;
+  TRY(pool_get(c, "dv_Sa", sizeof(double) * kmax * kmax, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dv_ev", sizeof(double) * kmax, &p)); ev = (double*)p;
+  TRY(pool_get(c, "dv_ework", sizeof(double) * 2 * kmax, &p)); ework = (double*)p;
+  TRY(pool_get(c, "dv_X", sizeof(double) * (size_t)N * m, &p)); X = (double*)p;
+  TRY(pool_get(c, "dv_WX", sizeof(double) * (size_t)N * m, &p)); WX = (double*)p;
+  TRY(pool_get(c, "dv_C", sizeof(double) * (size_t)N * m, &p)); Cc = (double*)p;
+  TRY(pool_get(c, "dv_E", sizeof(double) * m, &p)); E = (double*)p;
+  TRY(pool_get(c, "dv_nrm", sizeof(double) * m, &p)); nrm = (double*)p;
+  TRY(pool_get(c, "dv_tmp", sizeof(double) * (size_t)kmax * m, &p)); tmp = (double*)p;
+  TRY(pool_get(c, "dv_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
+  TRY(pool_get(c, "dv_Qw", sizeof(double) * Nk, &p)); Qw = (double*)p;
+  TRY(pool_get(c, "dv_tau", sizeof(double) * kmax, &p)); tau = (double*)p;
+  TRY(pool_get(c, "dv_info", sizeof(int), &p)); info = (int*)p;
+  cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
+  SS_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * NN, st));
+  scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
+                                               (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
+                                               (const int32_t*)c->d_ls.ptr, moy, H);
+  diag_kernel<<<(N + 255) / 256, 256, 0, st>>>(N, H, Hd);
+  // random normalised start vectors (src/davidson.F90:26-37), orthonormalised
+  gaussian_matrix_kernel<<<m, 256, 0, st>>>(1, 0x44415649u, N, m, U);
+  TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+  c->launches += 3;
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  std::vector<double> hE(m), hn(m);
+  bool converged = false;
+  int total = 0;
+  while (!converged && total < max_iter) {
+    int cols = m;  // columns of U in use
+    for (int iter = 1; iter <= nmax - 1 && !converged && total < max_iter; iter++, total++) {
+      const int shift = m * (iter - 1);
+      // W(:, shift:shift+m) = H U(:, shift:shift+m)
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, N, &one, H, N, U + (size_t)shift * N, N, &zero,
+                             WU + (size_t)shift * N, N));
+      const int k = shift + m;
+      // projected matrix S = U^T W (k x k), symmetrised, eigen-decomposed
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, k, N, &one, U, N, WU, N, &zero, S, k));
+      transpose_sym_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
+      TRY(sym_eig(st, k, Sa, ev, ework, info, &c->launches));
+      // lowest m Ritz vectors: columns 0..m-1 of Sa (row-major) -> tmp (k x m col-major)
+      c->launches += 1;
+      // copy eigenvector columns: Sa row-major (row i, col j) at i*k + j; tmp col-major (i, j) at i + j*k
+      std::vector<double> hv((size_t)k * k);
+      SS_CUDA_TRY(cudaMemcpyAsync(hv.data(), Sa, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(hE.data(), ev, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+      int hinfo = 0;
+      SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hinfo) {
+        ss_set_error_msg("davidson: projected eigenproblem did not converge");
+        return SS_ERR_NUMERIC;
+      }
+      std::vector<double> ht((size_t)k * m);
+      for (int j = 0; j < m; j++)
+        for (int i = 0; i < k; i++) ht[i + (size_t)j * k] = hv[(size_t)i * k + j];
+      SS_CUDA_TRY(cudaMemcpyAsync(tmp, ht.data(), sizeof(double) * k * m, cudaMemcpyHostToDevice, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(E, hE.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+      // X = U v, WX = W v (src/davidson.F90:118-126)
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, U, N, tmp, k, &zero, X, N));
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, WU, N, tmp, k, &zero, WX, N));
+      davidson_correction<<<nb((int64_t)N * m), 256, 0, st>>>(N, m, X, WX, E, Hd, Cc);
+      col_norms_kernel<<<m, 256, 0, st>>>(N, m, Cc, nrm);
+      c->launches += 2;
+      SS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaStreamSynchronize(st));
+      double mx = 0.0;
+      for (double v : hn) mx = std::max(mx, v);
+      converged = mx < tol;  // src/davidson.F90:143
+      if (converged || iter == nmax - 1) break;
+      // new block: corrections orthogonalised against U (twice) and among themselves
+      double* Un = U + (size_t)k * N;
+      SS_CUDA_TRY(cudaMemcpyAsync(Un, Cc, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, st));
+      for (int rep = 0; rep < 2; rep++) {
+        CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, m, N, &one, U, N, Un, N, &zero, tmp, k));
+        CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &mone, U, N, tmp, k, &one, Un, N));
+      }
+      TRY(ortho_qr(st, N, m, Un, N, Qw, tau, &c->launches));
+      cols = k + m;
+    }
+    (void)cols;
+    // restart with the current Ritz vectors (src/davidson.F90:151-155)
+    SS_CUDA_TRY(cudaMemcpyAsync(U, X, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, st));
+    TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+  }
+  if (!converged) {
+    ss_set_error_msg("davidson: not converged after %d iterations (largest correction %g)", max_iter,
+                     *std::max_element(hn.begin(), hn.end()));
+    return SS_ERR_NUMERIC;
+  }
+  if (evals) memcpy(evals, hE.data(), sizeof(double) * m);
+  if (evecs) SS_CUDA_TRY(cudaMemcpyAsync(evecs, X, sizeof(double) * N * m, cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  return SS_OK;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
 extern "C" {
-int ss_psd_clean(ss_ctx*, double*, int, int, int, int, uint64_t, int*) {
-  ss_set_error_msg("ss_psd_clean: not available in this build");
-  return SS_ERR_UNSUPPORTED;
+
+int ss_psd_clean(ss_ctx* c, double* moy, int layout, int rank, int oversample, int q, uint64_t seed,
+                 int* n_removed) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->n || !c->nint) {
+    ss_set_error_msg("basis and quartets must be set first");
+    return SS_ERR_STATE;
+  }
+  if (!moy || (layout != SS_LAYOUT_REF_N2 && layout != SS_LAYOUT_PACKED_PAIR) || rank < 1 || oversample < 0 ||
+      q < 0) {
+    ss_set_error_msg("ss_psd_clean: bad arguments");
+    return SS_ERR_ARG;
+  }
+  return psd_clean(c, moy, layout, rank, oversample, q, seed, n_removed);
 }
-int ss_davidson(ss_ctx*, const double*, int, int, double, int, double*, double*) {
-  ss_set_error_msg("ss_davidson: not available in this build");
-  return SS_ERR_UNSUPPORTED;
+
+int ss_psd_project(ss_ctx* c, double* moy, int layout, int* n_removed) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->n || !c->nint) {
+    ss_set_error_msg("basis and quartets must be set first");
+    return SS_ERR_STATE;
+  }
+  if (!moy || (layout != SS_LAYOUT_REF_N2 && layout != SS_LAYOUT_PACKED_PAIR)) {
+    ss_set_error_msg("ss_psd_project: bad arguments");
+    return SS_ERR_ARG;
+  }
+  return psd_project(c, moy, layout, n_removed);
 }
+
+int ss_davidson(ss_ctx* c, const double* moy, int layout, int m, double tol, int max_iter, double* evals,
+                double* evecs) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->n || !c->nint) {
+    ss_set_error_msg("basis and quartets must be set first");
+    return SS_ERR_STATE;
+  }
+  if (!moy || (layout != SS_LAYOUT_REF_N2 && layout != SS_LAYOUT_PACKED_PAIR) || !(tol > 0.0) || max_iter < 1) {
+    ss_set_error_msg("ss_davidson: bad arguments");
+    return SS_ERR_ARG;
+  }
+  return davidson(c, moy, layout, m, tol, max_iter, evals, evecs);
 }
+
+}  // extern "C"

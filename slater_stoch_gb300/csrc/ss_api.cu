@@ -354,6 +354,7 @@ void ss_destroy(ss_ctx* c) {
                     &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d};
   for (DevBuf* b : bufs) dev_free(c, *b);
   for (auto& kv : c->pool) dev_free(c, kv.second);
+  destroy_cublas(c->cublas_handle);
   cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -107,3 +107,29 @@ def test_library_loads_without_gpu():
         assert not h and L.ss_last_error()
     elif h:
         L.ss_destroy(h)
+
+
+def test_fortran_d_format():
+    from slater_stoch_gb300.output import fortran_d
+    assert fortran_d(0.0218344660055154) == " 0.218344660055154D-01"
+    assert fortran_d(-2.5) == "-0.250000000000000D+01"
+    assert fortran_d(0.0) == " 0.000000000000000D+00"
+    assert fortran_d(1.0) == " 0.100000000000000D+01"
+    assert len(fortran_d(-1.234e-20)) == 22
+
+
+def test_bielec_ao_round_trip(tmp_path):
+    from slater_stoch_gb300.output import read_bielec_ao, trexio_chunks, write_bielec_ao
+    q = basis.build_mapping(7)
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(len(q[0])) * 10.0 ** rng.integers(-20, 1, len(q[0]))
+    s = np.abs(rng.standard_normal(len(q[0]))) * 1e-9
+    write_bielec_ao(tmp_path / "bielec_ao", q, v, s)
+    idx, vv, ss = read_bielec_ao(tmp_path / "bielec_ao")
+    np.testing.assert_array_equal(idx, np.stack(q, axis=1))
+    np.testing.assert_allclose(vv, v, rtol=1e-14)
+    np.testing.assert_allclose(ss, s, rtol=1e-14)
+    line = (tmp_path / "bielec_ao").read_text().splitlines()[0]
+    assert len(line) == 4 * 6 + 2 * 22
+    chunks = list(trexio_chunks(q, v))
+    assert sum(len(c[2]) for c in chunks) == int(np.sum(np.abs(v) >= 1e-15))
