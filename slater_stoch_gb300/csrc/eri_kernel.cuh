@@ -24,6 +24,7 @@
 //    are run-to-run deterministic.
 #include <math.h>
 
+#include "boys.cuh"
 #include "ss_common.cuh"
 
 namespace ss {
@@ -161,56 +162,6 @@ __device__ __forceinline__ void axis_poly(const double* Pn, int degP, const doub
   }
 }
 
-static __constant__ double c_inv_odd[40] = {1.0 / 1.0, 1.0 / 3.0, 1.0 / 5.0, 1.0 / 7.0, 1.0 / 9.0, 1.0 / 11.0, 1.0 / 13.0, 1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0, 1.0 / 25.0, 1.0 / 27.0, 1.0 / 29.0, 1.0 / 31.0, 1.0 / 33.0, 1.0 / 35.0, 1.0 / 37.0, 1.0 / 39.0, 1.0 / 41.0, 1.0 / 43.0, 1.0 / 45.0, 1.0 / 47.0, 1.0 / 49.0, 1.0 / 51.0, 1.0 / 53.0, 1.0 / 55.0, 1.0 / 57.0, 1.0 / 59.0, 1.0 / 61.0, 1.0 / 63.0, 1.0 / 65.0, 1.0 / 67.0, 1.0 / 69.0, 1.0 / 71.0, 1.0 / 73.0, 1.0 / 75.0, 1.0 / 77.0, 1.0 / 79.0};  // 1/(2n+1)
-static __constant__ double c_inv_int[24] = {0.0, 1.0 / 1.0, 1.0 / 2.0, 1.0 / 3.0, 1.0 / 4.0, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0, 1.0 / 8.0, 1.0 / 9.0, 1.0 / 10.0, 1.0 / 11.0, 1.0 / 12.0, 1.0 / 13.0, 1.0 / 14.0, 1.0 / 15.0, 1.0 / 16.0, 1.0 / 17.0, 1.0 / 18.0, 1.0 / 19.0, 1.0 / 20.0, 1.0 / 21.0, 1.0 / 22.0, 1.0 / 23.0};  // 1/k (k >= 1)
-
-// Boys values F_0..F_nf(T) (nf <= NF).  T >= 1: the reference's erf + upward recursion
-// (src/rint_sum.F90:44-61), with erf(sqrt T) == 1 exactly for T > 36; T < 1: the Taylor series
-// of src/rint1.F90 for F_nf only, then the stable downward recursion
-// F_n = (2T F_{n+1} + e^-T)/(2n+1) (differs from the per-n Taylor sums by < 1e-15 relative).
-template <int NF>
-__device__ __forceinline__ void boys(double T, int nf, double (&F)[NF + 1]) {
-  const double sqpi = 1.7724538509055160273;  // dsqrt(dacos(-1.d0))
-  if (T < 1.0) {
-    if (T == 0.0) {
-#pragma unroll
-      for (int n = 0; n <= NF; n++) F[n] = c_inv_odd[n];
-      return;
-    }
-    double ck = 1.0, s = c_inv_odd[nf];
-#pragma unroll 1
-    for (int k = 1; k <= 22; k++) {
-      ck = ck * (-T) * c_inv_int[k];
-      const double term = ck * c_inv_odd[nf + k];
-      s = s + term;
-      if (abs_lt(term, 1.e-17)) break;
-    }
-    const double e = exp(-T);
-    F[NF] = 0.0;
-#pragma unroll
-    for (int n = NF; n >= 0; n--) {
-      if (n == nf) F[n] = s;
-      else if (n < nf) F[n] = fma(T + T, F[n + 1 <= NF ? n + 1 : NF], e) * c_inv_odd[n];
-    }
-  } else {
-    const double v = (T > 80.0) ? 0.0 : exp(-T);
-    const double u_inv = 1.0 / sqrt(T);
-    const double u = T * u_inv;
-    const double two_rho_inv = 0.5 * u_inv * u_inv;
-    const double val0 = 0.5 * u_inv * sqpi * (T > 36.0 ? 1.0 : erf(u));
-    F[0] = val0;
-    double rt = (val0 - v) * two_rho_inv;
-    double di = 3.0;
-#pragma unroll
-    for (int n = 1; n <= NF; n++) {
-      if (n > nf) break;
-      F[n] = rt;
-      rt = (rt * di - v) * two_rho_inv;
-      di = di + 2.0;
-    }
-  }
-}
-
 // Work per CTA: one function quartet (ik|jl) and a slice of its bra primitive pairs against all
 // its ket primitive pairs, the ket pairs staged in shared memory in tiles together with their
 // recentred polynomials.  Items (bra pair, ket pair) are dealt round-robin to the threads, so
@@ -229,6 +180,8 @@ __global__ void __launch_bounds__(128) eri_kernel(
   PrimPair* s_ket = reinterpret_cast<PrimPair*>(s_raw);
   double* s_q = reinterpret_cast<double*>(s_ket + ktile);
   __shared__ double s_red[4];
+  __shared__ double s_boys[BOYS_SMEM_DOUBLES];
+  boys_tables_to_smem(s_boys);  // ordered before first use by the tile loop's barriers
 
   const int64_t w = blockIdx.x / split;
   const int part = blockIdx.x % split;
@@ -311,7 +264,8 @@ __global__ void __launch_bounds__(128) eri_kernel(
       const double p = P.p, qq = Q.p;
       // src/general_primitive_integral.F90:54-60, 142-146
       const double pq = P.p_inv * 0.5 * Q.p_inv;
-      const double pq_inv = 0.5 / (p + qq);
+      const double rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
+      const double pq_inv = 0.5 * (rs_pq * rs_pq);
       RecCoef R;
       R.p10_1 = qq * pq;
       R.p01_1 = p * pq;
@@ -323,7 +277,7 @@ __global__ void __launch_bounds__(128) eri_kernel(
       const double dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
       const double T = (dx * dx + dy * dy + dz * dz) * rho;
       double F[NF + 1];
-      boys<NF>(T, nf, F);
+      boys_tab<NF>(T, nf, F, s_boys);
 
       double accu;
       if (!T2) {
@@ -445,7 +399,7 @@ __global__ void __launch_bounds__(128) eri_kernel(
               }
       }
       // src/general_primitive_integral.F90:192 and the coefficient product of src/gauss_ijkl.F90:137
-      const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv / sqrt(p + qq);
+      const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
       acc = fma(P.coef * Q.coef, pref * accu, acc);
       // next item of this thread
       ik += blockDim.x;

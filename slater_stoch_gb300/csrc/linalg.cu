@@ -109,7 +109,7 @@ int ortho_qr(cudaStream_t st, int N, int r, double* Z, int ld, double* Qwork, do
 __global__ void __launch_bounds__(1024) sym_eig_kernel(int n, double* __restrict__ a, double* __restrict__ d,
                                                        double* __restrict__ e, int* __restrict__ info) {
   __shared__ double sh[32];
-  __shared__ double s_f, s_hh;
+  __shared__ double s_f, s_hh, s_anorm;
   __shared__ double s_c[1024], s_s[1024];
   __shared__ int s_m, s_cnt, s_stop;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -202,6 +202,9 @@ __global__ void __launch_bounds__(1024) sym_eig_kernel(int n, double* __restrict
     for (int i = 1; i < n; i++) e[i - 1] = e[i];
     e[n - 1] = 0.0;
     *info = 0;
+    double an = 0.0;
+    for (int i = 0; i < n; i++) an = fmax(an, fabs(d[i]) + fabs(e[i]));
+    s_anorm = an;
   }
   __syncthreads();
   for (int l = 0; l < n; l++) {
@@ -211,7 +214,11 @@ __global__ void __launch_bounds__(1024) sym_eig_kernel(int n, double* __restrict
         int m;
         for (m = l; m < n - 1; m++) {
           const double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= 2.2204460492503131e-16 * dd) break;
+          // split where e[m] is negligible next to its diagonal neighbours or to the whole
+          // matrix (the absolute test deflates blocks of rounding-level entries, e.g. the
+          // numerical null space of a rank-deficient Coulomb metric, that the relative test
+          // alone would iterate on without converging)
+          if (fabs(e[m]) <= 2.2204460492503131e-16 * dd || fabs(e[m]) <= 2.2204460492503131e-16 * s_anorm) break;
         }
         s_m = m;
         s_cnt = 0;

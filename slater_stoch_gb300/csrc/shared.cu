@@ -89,14 +89,17 @@ __global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, Mi
 // delta_i = poly_i (u_orb_i - u_gauss_i).  With 20-Gaussian fits delta/phi is 1e-5..1e-8, so the
 // residual is formed in FP64 (a difference of two FP32 values would be rounding noise); Gaussian
 // terms whose exponent exceeds the most diffuse term's by more than 60 (relative size < 1e-26
-// times a coefficient ratio) are skipped.  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
-__global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, const double* __restrict__ u1,
-                                         const double* __restrict__ u2, float* __restrict__ out) {
+// times a coefficient ratio) are skipped.  The radial parts are evaluated once per shell (the
+// consecutive functions sharing centre, STO exponent and fit, which differ only by their
+// cartesian monomial).  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
+__global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, const int* __restrict__ shell_start,
+                                         const double* __restrict__ u1, const double* __restrict__ u2,
+                                         float* __restrict__ out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int i = blockIdx.y;
+  const int sh = blockIdx.y;
   if (s >= S) return;
+  const int i = shell_start[sh], i_end = shell_start[sh + 1];
   const double* A = B.center + 3 * i;
-  const int px = B.npower[3 * i], py = B.npower[3 * i + 1], pz = B.npower[3 * i + 2];
   const int nsto = B.n_sto[i];
   const double zeta = B.g_slater[i];
   const int ng = B.n_gauss[i];
@@ -110,10 +113,6 @@ __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, cons
   for (int e = 0; e < 2; e++) {
     const double* u = e == 0 ? u1 : u2;
     const double dx = u[3 * s] - A[0], dy = u[3 * s + 1] - A[1], dz = u[3 * s + 2] - A[2];
-    double poly = 1.0;
-    for (int t = 0; t < px; t++) poly *= dx;
-    for (int t = 0; t < py; t++) poly *= dy;
-    for (int t = 0; t < pz; t++) poly *= dz;
     const double r2 = dx * dx + dy * dy + dz * dz;
     const double r = sqrt(r2);
     double uo = exp(-zeta * r);
@@ -125,10 +124,17 @@ __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, cons
       if ((float)gg[m] * r2f > ycut) continue;
       ug += (c1[m] + c2[m] * r2) * exp(-gg[m] * r2);
     }
-    const int64_t o = (int64_t)i * ld + s;
-    out[(3 * e) * plane + o] = (float)(poly * uo);
-    out[(3 * e + 1) * plane + o] = (float)(poly * ug);
-    out[(3 * e + 2) * plane + o] = (float)(poly * (uo - ug));
+    const double res = uo - ug;
+    for (int f = i; f < i_end; f++) {
+      double poly = 1.0;
+      for (int t = 0; t < B.npower[3 * f]; t++) poly *= dx;
+      for (int t = 0; t < B.npower[3 * f + 1]; t++) poly *= dy;
+      for (int t = 0; t < B.npower[3 * f + 2]; t++) poly *= dz;
+      const int64_t o = (int64_t)f * ld + s;
+      out[(3 * e) * plane + o] = (float)(poly * uo);
+      out[(3 * e + 1) * plane + o] = (float)(poly * ug);
+      out[(3 * e + 2) * plane + o] = (float)(poly * res);
+    }
   }
 }
 
@@ -218,8 +224,25 @@ struct SharedPlan {
   int npairs = 0;
   std::vector<int> pi, pk, p1, p2;  // used pairs; per-quartet pair indices
   int* d_pi = nullptr; int* d_pk = nullptr; int* d_p1 = nullptr; int* d_p2 = nullptr;
+  std::vector<int> shell_start;     // consecutive functions with identical radial part
+  int* d_shell = nullptr;
   MixDev mix{};
 };
+
+static bool same_radial(const ss_ctx* c, int a, int b) {
+  if (c->h_nsto[a] != c->h_nsto[b] || c->h_itype[a] != c->h_itype[b] || c->h_ng[a] != c->h_ng[b] ||
+      c->h_gs[a] != c->h_gs[b])
+    return false;
+  for (int l = 0; l < 3; l++)
+    if (c->h_center[3 * a + l] != c->h_center[3 * b + l]) return false;
+  const size_t ld = c->ld, n = c->n;
+  for (int m = 0; m < c->h_ng[a]; m++) {
+    if (c->h_gg[m + ld * a] != c->h_gg[m + ld * b]) return false;
+    for (int t = 0; t < 2; t++)
+      if (c->h_cg[m + ld * (a + n * t)] != c->h_cg[m + ld * (b + n * t)]) return false;
+  }
+  return true;
+}
 
 static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
   const int n = c->n;
@@ -279,6 +302,11 @@ static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
   TRY(upload_v(c, "sh_pk", S.pk, &S.d_pk));
   TRY(upload_v(c, "sh_p1", S.p1, &S.d_p1));
   TRY(upload_v(c, "sh_p2", S.p2, &S.d_p2));
+  S.shell_start.assign(1, 0);
+  for (int f = 1; f < c->n; f++)
+    if (!same_radial(c, f, S.shell_start.back())) S.shell_start.push_back(f);
+  S.shell_start.push_back(c->n);
+  TRY(upload_v(c, "sh_shell", S.shell_start, &S.d_shell));
   return SS_OK;
 }
 
@@ -333,8 +361,8 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
       const int64_t first = (int64_t)b * npts + c0;
       shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, u1, u2, w);
       SS_CUDA_TRY(cudaGetLastError());
-      shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)n), 128, 0, c->stream>>>(
-          c->basis, ns, Sc, u1, u2, F);
+      shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)(SP.shell_start.size() - 1)), 128, 0,
+                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, u1, u2, F);
       SS_CUDA_TRY(cudaGetLastError());
       shared_operand_kernel<<<dim3((unsigned)((Kh + 255) / 256), (unsigned)P), 256, 0, c->stream>>>(
           ns, Kh, Sc, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);

@@ -71,6 +71,26 @@ def test_psd_project_exact(cfg, layout):
         assert np.linalg.eigvalsh(OC.matrix_from_eris(got, q, b.n, layout)).min() >= -1e-12
 
 
+def test_psd_project_rank_deficient_metric():
+    """The exact analytic Coulomb metric of the H2O 26-function basis is PSD with a numerical
+    null space (eigenvalues at rounding level, ~1e-16 of the largest); its tridiagonal form
+    carries a long run of rounding-level entries that the eigensolver must deflate."""
+    from oracle import cleanup as OC
+    b = configs.h2o_26(ng0=6)
+    q = basis.build_mapping(b.n)
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*q)
+        g, _ = ctx.gauss_eri()
+        got, nrem = ctx.psd_project(g, layout="packed_pair")
+    ev = np.linalg.eigvalsh(OC.matrix_from_eris(g, q, b.n, "packed_pair"))
+    assert ev.min() > -1e-13 * ev.max()  # the input is PSD to rounding
+    # only rounding-level components are removed (their signs are noise, so their count is not
+    # compared with numpy's)
+    assert 0 <= nrem < len(ev)
+    assert np.max(np.abs(got - g)) <= 1e-13 * np.abs(g).max()
+
+
 def test_clean_pipeline_is_psd():
     """svd_clean (the benchmark spec parameters: rank 200, oversampling 10, 4 power iterations on the
     351x351 packed metric) followed by the exact projection: PSD to -1e-12."""
