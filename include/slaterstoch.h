@@ -106,6 +106,18 @@ int ss_combine(ss_ctx* ctx, double* out);
 int ss_two_e_job(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
                  int estimator, int precision, double sigma_target, double* eri, double* sigma);
 
+/* Asynchronous job API (the reference runs one job per process and has none; these queue the
+ * job of ss_two_e_job for a serving caller).  ss_job_submit copies the context's basis and
+ * quartets and returns at once; the job runs on a worker thread with a private context on the
+ * same device, so several jobs overlap on the GPU and later calls on ctx do not affect them.
+ * ss_job_poll sets *done = 1 once the job finished; ss_job_result waits for it, copies its eri
+ * and sigma (nint each, may be NULL) and forgets the job, returning the job's status code.
+ * ss_destroy waits for unfinished jobs and drops their results. */
+int ss_job_submit(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
+                  int estimator, int precision, double sigma_target, int64_t* job_id);
+int ss_job_poll(ss_ctx* ctx, int64_t job_id, int* done);
+int ss_job_result(ss_ctx* ctx, int64_t job_id, double* eri, double* sigma);
+
 /* Drop cached device results (Schwarz diagonal, analytic ERIs, MC sums); inputs stay. */
 int ss_invalidate(ss_ctx* ctx);
 

@@ -41,6 +41,10 @@ SIGNATURES = {
     "ss_combine": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ss_two_e_job": (C.c_int, [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_int, C.c_int, C.c_int,
                                C.c_double, C.c_void_p, C.c_void_p]),
+    "ss_job_submit": (C.c_int, [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                C.c_double, C.c_void_p]),
+    "ss_job_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "ss_job_result": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "ss_invalidate": (C.c_int, [C.c_void_p]),
     "ss_mc_max_sigma": (C.c_double, [C.c_void_p]),
     "ss_mc_blocks_done": (C.c_int, [C.c_void_p]),

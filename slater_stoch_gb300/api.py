@@ -137,6 +137,28 @@ class Context:
                                         float(sigma_target), _ptr(eri), _ptr(sig)))
         return eri, sig
 
+    # -- asynchronous jobs -----------------------------------------------------------
+    def job_submit(self, a_zv: float, seed: int, npts: int, nblocks: int, estimator: str = "shared",
+                   precision: str = "split_bf16", sigma_target: float = 0.0) -> int:
+        """Queue the job of two_e_job on a worker thread (inputs copied now); returns its id."""
+        jid = np.zeros(1, np.int64)
+        _lib.check(self._L.ss_job_submit(self._h, float(a_zv), int(seed), int(npts), int(nblocks),
+                                         ESTIMATORS[estimator], PRECISIONS[precision],
+                                         float(sigma_target), _ptr(jid)))
+        return int(jid[0])
+
+    def job_poll(self, job_id: int) -> bool:
+        done = np.zeros(1, np.int32)
+        _lib.check(self._L.ss_job_poll(self._h, int(job_id), _ptr(done)))
+        return bool(done[0])
+
+    def job_result(self, job_id: int):
+        """Wait for the job; (eri, sigma).  Raises with the job's own error if it failed."""
+        eri = np.zeros(self.nint)
+        sig = np.zeros(self.nint)
+        _lib.check(self._L.ss_job_result(self._h, int(job_id), _ptr(eri), _ptr(sig)))
+        return eri, sig
+
     def invalidate(self):
         _lib.check(self._L.ss_invalidate(self._h))
 

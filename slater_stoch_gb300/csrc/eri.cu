@@ -101,7 +101,9 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
       }
       r.coef = B.c_gauss[m1 + (int64_t)B.ld * (i + (int64_t)B.n * ti)] *
                B.c_gauss[m2 + (int64_t)B.ld * (k + (int64_t)B.n * tk)];
-      r.pad[0] = r.pad[1] = r.pad[2] = 0.0;
+      r.pad[0] = 0.0;                    // Schwarz factor, set by the ERI kernel's self mode
+      r.pad[1] = (double)(m1 * ngk + m2);  // position in the reference's (m1, m2) loop
+      r.pad[2] = 0.0;
       out[o++] = r;
     }
 }
@@ -149,35 +151,79 @@ cudaError_t eri_init_constants() { return cudaSuccess; }  // tables are compile-
 void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
   const int no = t2 ? 4 : 1;
   const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (L + 1);
-  int kt = (int)((200u * 1024u) / per);
+  // Classes with r^2-type fits keep their per-item recursion tables and option polynomials in
+  // local memory: a small ket tile leaves the SM's unified L1 to them (measured on the 26-function
+  // H2O basis: 200 KB -> 40 KB tiles took these classes from 3.6 s to 2.7 s).  The other classes
+  // keep their working set in registers and take the largest tile.
+  const size_t budget = (t2 ? 40u : 200u) * 1024u;
+  int kt = (int)(budget / per);
   kt = kt < max_cnt ? kt : max_cnt;
   kt = kt < 1 ? 1 : kt;
   *ktile = kt;
   *smem = per * kt;
 }
 
-cudaError_t launch_eri_L0n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L1n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L2n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L3n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L4n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L2t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L3t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
-cudaError_t launch_eri_L4t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, double*);
+cudaError_t launch_eri_L0n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L1n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L2n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L3n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L2t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L3t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
 
 cudaError_t launch_eri_class(int L, bool t2, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
-                             const int32_t* ks, const int32_t* ls, double* partial) {
-  if (L == 0 && t2 == false) return launch_eri_L0n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 1 && t2 == false) return launch_eri_L1n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 2 && t2 == false) return launch_eri_L2n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 3 && t2 == false) return launch_eri_L3n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 4 && t2 == false) return launch_eri_L4n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 2 && t2 == true) return launch_eri_L2t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 3 && t2 == true) return launch_eri_L3t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
-  if (L == 4 && t2 == true) return launch_eri_L4t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, partial);
+                             const int32_t* ks, const int32_t* ls, const double* pre, double eps,
+                             double* partial, double* self_out) {
+  if (L == 0 && t2 == false) return launch_eri_L0n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 1 && t2 == false) return launch_eri_L1n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 2 && t2 == false) return launch_eri_L2n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 3 && t2 == false) return launch_eri_L3n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 4 && t2 == false) return launch_eri_L4n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 2 && t2 == true) return launch_eri_L2t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 3 && t2 == true) return launch_eri_L3t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (L == 4 && t2 == true) return launch_eri_L4t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
   return cudaErrorInvalidValue;
+}
+
+// Sort the primitive pairs of every function pair by decreasing Schwarz factor (pad[0]), ties
+// by the reference's loop position (pad[1]), so the order is a function of the values alone.
+// One CTA per function pair, bitonic sort of up to 1024 keys in shared memory; out = sorted copy.
+__global__ void __launch_bounds__(512) prim_pair_sort(const PrimPair* __restrict__ in, const int64_t* __restrict__ off,
+                                                      const int* __restrict__ cnt, PrimPair* __restrict__ out) {
+  __shared__ double s_key[1024], s_pos[1024];
+  __shared__ int s_idx[1024];
+  const int pidx = blockIdx.x;
+  const int m = cnt[pidx];
+  const PrimPair* src = in + off[pidx];
+  PrimPair* dst = out + off[pidx];
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) {
+    s_key[t] = t < m ? src[t].pad[0] : -1.0;  // padding sorts last
+    s_pos[t] = t < m ? src[t].pad[1] : 1.0e300;
+    s_idx[t] = t;
+  }
+  __syncthreads();
+  // "a before b": larger key first, then smaller reference position
+  for (int k = 2; k <= 1024; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < 1024; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const bool up = (t & k) == 0;
+          const bool t_first = s_key[t] > s_key[u] || (s_key[t] == s_key[u] && s_pos[t] < s_pos[u]);
+          if (up != t_first) {
+            const double kk = s_key[t], pp2 = s_pos[t];
+            const int ii = s_idx[t];
+            s_key[t] = s_key[u]; s_pos[t] = s_pos[u]; s_idx[t] = s_idx[u];
+            s_key[u] = kk; s_pos[u] = pp2; s_idx[u] = ii;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) dst[t] = src[s_idx[t]];
 }
 
 }  // namespace ss

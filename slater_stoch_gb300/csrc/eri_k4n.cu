@@ -5,10 +5,12 @@ namespace ss {
 cudaError_t launch_eri_L4n(dim3 grid, int ktile, size_t smem, cudaStream_t st, const BasisDev& B,
                               const PrimPair* pp, const int64_t* off, const int* cnt, const int64_t* work,
                               int split, const int32_t* is, const int32_t* js, const int32_t* ks,
-                              const int32_t* ls, double* partial) {
+                              const int32_t* ls, const double* pre, double eps, double* partial,
+                              double* self_out) {
   cudaError_t e = cudaFuncSetAttribute(eri_kernel<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  eri_kernel<4, false><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, partial);
+  eri_kernel<4, false><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, pre, eps, partial,
+                                              self_out);
   return cudaGetLastError();
 }
 }  // namespace ss

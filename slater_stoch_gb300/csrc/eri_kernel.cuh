@@ -162,24 +162,240 @@ __device__ __forceinline__ void axis_poly(const double* Pn, int degP, const doub
   }
 }
 
+// CTA-uniform description of one function quartet (ik|jl): cartesian powers, which functions
+// are r^2-type fits, the Boys order and the per-axis maximal degrees of bra and ket.
+struct QuartetShape {
+  int np[4][3];
+  int t2[4];
+  int nf;
+  int amax[3], cmax[3];
+};
+
+template <bool T2>
+__device__ __forceinline__ QuartetShape quartet_shape(const BasisDev& B, int fi, int fk, int fj, int fl) {
+  QuartetShape S;
+  const int fn[4] = {fi, fk, fj, fl};
+  S.nf = 0;
+#pragma unroll
+  for (int f = 0; f < 4; f++) {
+    S.t2[f] = T2 ? (B.i_type[fn[f]] == 2) : 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      S.np[f][ax] = B.npower[3 * fn[f] + ax];
+      S.nf += S.np[f][ax];
+    }
+    S.nf += 2 * S.t2[f];
+  }
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++) {
+    S.amax[ax] = S.np[0][ax] + S.np[1][ax] + 2 * (S.t2[0] + S.t2[1]);
+    S.cmax[ax] = S.np[2][ax] + S.np[3][ax] + 2 * (S.t2[2] + S.t2[3]);
+  }
+  return S;
+}
+
+// recentred pair polynomials of a primitive pair, per (axis, option); side 0 = bra (functions
+// i, k), side 1 = ket (functions j, l).  Layout [ax][o][L+1].
+template <int L, bool T2>
+__device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, const PrimPair& P, double* out) {
+  constexpr int NO = T2 ? 4 : 1;
+  const int f0 = 2 * side, f1 = 2 * side + 1;
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++)
+#pragma unroll
+    for (int o = 0; o < NO; o++) {
+      if ((o & 1) && !S.t2[f0]) continue;
+      if ((o & 2) && !S.t2[f1]) continue;
+      pair_poly<L>(P.PA[ax], S.np[f0][ax] + 2 * (o & 1), P.PB[ax], S.np[f1][ax] + (o & 2),
+                   out + (ax * NO + o) * (L + 1));
+    }
+}
+
+// One primitive quartet (src/general_primitive_integral.F90, summed over the cartesian
+// components of the r^2-type fits): returns pref * sum_n d1[n] F_n; the caller multiplies by
+// the coefficient product P.coef * Q.coef.  Pn, Qn: pair_polys of the bra and ket pairs.
+template <int L, bool T2>
+__device__ __forceinline__ double prim_quartet(const QuartetShape& S, const PrimPair& P, const double* Pn,
+                                               const PrimPair& Q, const double* Qn, const double* s_boys) {
+  constexpr int NO = T2 ? 4 : 1;
+  constexpr int NF = (6 * L < 16) ? 6 * L : 16;
+  const double p = P.p, qq = Q.p;
+  // src/general_primitive_integral.F90:54-60, 142-146
+  const double pq = P.p_inv * 0.5 * Q.p_inv;
+  const double rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
+  const double pq_inv = 0.5 * (rs_pq * rs_pq);
+  RecCoef R;
+  R.p10_1 = qq * pq;
+  R.p01_1 = p * pq;
+  const double pq_inv_2 = pq_inv + pq_inv;
+  R.p10_2 = pq_inv_2 * R.p10_1 * qq;
+  R.p01_2 = pq_inv_2 * R.p01_1 * p;
+  R.pq_inv = pq_inv;
+  const double rho = p * qq * pq_inv_2;
+  const double dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
+  const double T = (dx * dx + dy * dy + dz * dz) * rho;
+  double F[NF + 1];
+  boys_tab<NF>(T, S.nf, F, s_boys);
+  const int nf = S.nf;
+
+  double accu;
+  if (!T2) {
+    double A[3][2 * L + 1];
+    int deg[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      deg[ax] = S.amax[ax] + S.cmax[ax];
+      if (deg[ax] == 0) {
+        A[ax][0] = 1.0;
+#pragma unroll
+        for (int m = 1; m <= 2 * L; m++) A[ax][m] = 0.0;
+        continue;
+      }
+      double I[L + 1][L + 1][2 * L + 1];
+      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
+      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
+      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      axis_poly<L>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (L + 1), S.cmax[ax], I, ax == 0, A[ax]);
+    }
+    // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
+    double dp[4 * L + 1];
+#pragma unroll
+    for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
+#pragma unroll
+    for (int a = 0; a <= 2 * L; a++) {
+      if (a > deg[0]) break;
+#pragma unroll
+      for (int c = 0; c <= 2 * L; c++) {
+        if (c > deg[1]) break;
+        dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
+      }
+    }
+    double d1[NF + 1];
+#pragma unroll
+    for (int t = 0; t <= NF; t++) d1[t] = 0.0;
+#pragma unroll
+    for (int a = 0; a <= 4 * L; a++) {
+      if (a > deg[0] + deg[1] || a > NF) break;
+#pragma unroll
+      for (int c = 0; c <= 2 * L; c++) {
+        if (c > deg[2] || a + c > NF) break;
+        d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
+      }
+    }
+    accu = d1[0] * F[0];
+#pragma unroll
+    for (int n = 1; n <= NF; n++)
+      if (n <= nf) accu = fma(d1[n], F[n], accu);
+  } else {
+    // axis polynomials for every (bra option, ket option), then the cartesian combinations
+    double A[3][NO * NO][2 * L + 1];
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ax++) {
+      double I[L + 1][L + 1][2 * L + 1];
+      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
+      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
+      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+#pragma unroll 1
+      for (int ob = 0; ob < NO; ob++) {
+        if ((ob & 1) && !S.t2[0]) continue;
+        if ((ob & 2) && !S.t2[1]) continue;
+#pragma unroll 1
+        for (int oc = 0; oc < NO; oc++) {
+          if ((oc & 1) && !S.t2[2]) continue;
+          if ((oc & 2) && !S.t2[3]) continue;
+          const int da = S.np[0][ax] + S.np[1][ax] + 2 * (ob & 1) + (ob & 2);
+          const int dc = S.np[2][ax] + S.np[3][ax] + 2 * (oc & 1) + (oc & 2);
+          axis_poly<L>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0,
+                       A[ax][ob * NO + oc]);
+        }
+      }
+    }
+    accu = 0.0;
+    const int nci = S.t2[0] ? 3 : 1, nck = S.t2[1] ? 3 : 1, ncj = S.t2[2] ? 3 : 1, ncl = S.t2[3] ? 3 : 1;
+    for (int ci = 0; ci < nci; ci++)
+      for (int ck = 0; ck < nck; ck++)
+        for (int cj = 0; cj < ncj; cj++)
+          for (int cl = 0; cl < ncl; cl++) {
+            int sel[3], deg[3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+              const int ob = (S.t2[0] && ci == ax ? 1 : 0) | (S.t2[1] && ck == ax ? 2 : 0);
+              const int oc = (S.t2[2] && cj == ax ? 1 : 0) | (S.t2[3] && cl == ax ? 2 : 0);
+              sel[ax] = ob * NO + oc;
+              deg[ax] = S.np[0][ax] + S.np[1][ax] + S.np[2][ax] + S.np[3][ax] +
+                        2 * ((ob & 1) + (ob >> 1) + (oc & 1) + (oc >> 1));
+            }
+            const double* Ax = A[0][sel[0]];
+            const double* Ay = A[1][sel[1]];
+            const double* Az = A[2][sel[2]];
+            double dp[4 * L + 1];
+#pragma unroll
+            for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
+#pragma unroll
+            for (int a = 0; a <= 2 * L; a++) {
+              if (a > deg[0]) break;
+#pragma unroll
+              for (int c = 0; c <= 2 * L; c++) {
+                if (c > deg[1]) break;
+                dp[a + c] = fma(Ay[c], Ax[a], dp[a + c]);
+              }
+            }
+            double d1[NF + 1];
+#pragma unroll
+            for (int t = 0; t <= NF; t++) d1[t] = 0.0;
+#pragma unroll
+            for (int a = 0; a <= 4 * L; a++) {
+              if (a > deg[0] + deg[1] || a > NF) break;
+#pragma unroll
+              for (int c = 0; c <= 2 * L; c++) {
+                if (c > deg[2] || a + c > NF) break;
+                d1[a + c] = fma(Az[c], dp[a], d1[a + c]);
+              }
+            }
+            double sum = d1[0] * F[0];
+#pragma unroll
+            for (int n = 1; n <= NF; n++)
+              if (n <= nf) sum = fma(d1[n], F[n], sum);
+            accu = accu + sum;
+          }
+  }
+  // src/general_primitive_integral.F90:192
+  const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
+  return pref * accu;
+}
+
 // Work per CTA: one function quartet (ik|jl) and a slice of its bra primitive pairs against all
 // its ket primitive pairs, the ket pairs staged in shared memory in tiles together with their
-// recentred polynomials.  Items (bra pair, ket pair) are dealt round-robin to the threads, so
-// every thread does the same number of primitive quartets.
+// recentred polynomials.
+//
+// Primitive screening (pre != nullptr): the primitive pairs of every function pair are sorted
+// by decreasing Schwarz factor S; a primitive quartet with S_P S_Q < eps sqrt((ik|ik)(jl|jl))
+// is skipped.  Each skipped term is bounded by that product, so the skipped part of an ERI is at
+// most (number of primitive quartets) * eps * sqrt((ik|ik)(jl|jl)).  For each bra pair the kept
+// ket pairs of a tile are a prefix of the tile; the kept items of the tile are numbered through
+// an exclusive scan of the per-bra prefix lengths.  Without pre every item is kept (the Schwarz
+// diagonal itself).  The items are spread evenly over the threads (to within one).
+//
+// Schwarz-factor mode (self_out != nullptr; work = the quartets (ik|ik)): only the items (P, P)
+// are evaluated and S_P = sqrt(c_P^2 (P|P)), the self-repulsion of the primitive pair's charge
+// distribution (summed over the cartesian components of r^2-type fits) times its coefficient,
+// is written to self_out[16 * (pair_off + P)] (PrimPair::pad[0] of the pair).  By
+// Cauchy-Schwarz |c_P c_Q (P|Q)| <= S_P S_Q for every primitive quartet.
 // T2: some of the four functions are r^2-type fits (3 cartesian components sharing exponents).
 template <int L, bool T2>
 __global__ void __launch_bounds__(128) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
     const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
-    const int32_t* __restrict__ ls, double* __restrict__ partial) {
+    const int32_t* __restrict__ ls, const double* __restrict__ pre, double eps, double* __restrict__ partial,
+    double* __restrict__ self_out) {
   constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
-  constexpr int NF = (6 * L < 16) ? 6 * L : 16;
   constexpr int QW = 3 * NO * (L + 1);  // ket polynomial doubles per ket pair
   extern __shared__ double2 s_raw[];
   PrimPair* s_ket = reinterpret_cast<PrimPair*>(s_raw);
   double* s_q = reinterpret_cast<double*>(s_ket + ktile);
   __shared__ double s_red[4];
+  __shared__ int s_scan[SS_MAX_NG * SS_MAX_NG + 1];  // kept-item offsets of the bra slice
   __shared__ double s_boys[BOYS_SMEM_DOUBLES];
   boys_tables_to_smem(s_boys);  // ordered before first use by the tile loop's barriers
 
@@ -191,31 +407,14 @@ __global__ void __launch_bounds__(128) eri_kernel(
   const int nb = pair_cnt[pb], nk = pair_cnt[pk];
   const PrimPair* bra = pp + pair_off[pb];
   const PrimPair* ket = pp + pair_off[pk];
-
-  int np[4][3], t2[4];
-  const int fn[4] = {fi, fk, fj, fl};
-  int nf = 0;
-#pragma unroll
-  for (int f = 0; f < 4; f++) {
-    t2[f] = T2 ? (B.i_type[fn[f]] == 2) : 0;
-#pragma unroll
-    for (int ax = 0; ax < 3; ax++) {
-      np[f][ax] = B.npower[3 * fn[f] + ax];
-      nf += np[f][ax];
-    }
-    nf += 2 * t2[f];
-  }
-  // per axis: powers of each option and maximal degrees
-  int amax[3], cmax[3];
-#pragma unroll
-  for (int ax = 0; ax < 3; ax++) {
-    amax[ax] = np[0][ax] + np[1][ax] + 2 * (t2[0] + t2[1]);
-    cmax[ax] = np[2][ax] + np[3][ax] + 2 * (t2[2] + t2[3]);
-  }
+  const QuartetShape S = quartet_shape<T2>(B, fi, fk, fj, fl);
+  const int n = B.n;
+  const double tau = pre ? eps * sqrt(pre[fi + (int64_t)n * fk] * pre[fj + (int64_t)n * fl]) : 0.0;
 
   const int per = (nb + split - 1) / split;
   const int b0 = part * per;
   const int b1 = min(nb, b0 + per);
+  const int nbs = max(b1 - b0, 0);
   double acc = 0.0;
 
   for (int t0 = 0; t0 < nk; t0 += ktile) {
@@ -227,186 +426,67 @@ __global__ void __launch_bounds__(128) eri_kernel(
     }
     __syncthreads();
     // recentred ket polynomials, per (ket pair, axis, option)
-    for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) {
-      const PrimPair& Q = s_ket[kk];
-#pragma unroll
-      for (int ax = 0; ax < 3; ax++)
-#pragma unroll
-        for (int o = 0; o < NO; o++) {
-          if ((o & 1) && !t2[2]) continue;
-          if ((o & 2) && !t2[3]) continue;
-          pair_poly<L>(Q.PA[ax], np[2][ax] + 2 * (o & 1), Q.PB[ax], np[3][ax] + (o & 2),
-                       s_q + (size_t)kk * QW + (ax * NO + o) * (L + 1));
+    for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) pair_polys<L, T2>(S, 1, s_ket[kk], s_q + (size_t)kk * QW);
+    // kept ket prefix of every bra pair of the slice (ket factors decrease along the tile)
+    for (int bi = threadIdx.x; bi < nbs; bi += blockDim.x) {
+      int c = kt;
+      if (self_out) {
+        c = (b0 + bi >= t0 && b0 + bi < t0 + kt) ? 1 : 0;  // the item (P, P) lies in this tile
+      } else if (tau > 0.0) {
+        const double sb = bra[b0 + bi].pad[0];
+        if (sb * s_ket[0].pad[0] < tau) {
+          c = 0;
+        } else {
+          int lo = 1, hi = kt;  // first index with sb * S_Q < tau lies in [lo, hi]
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sb * s_ket[mid].pad[0] < tau) hi = mid; else lo = mid + 1;
+          }
+          c = lo;
         }
+      }
+      s_scan[bi + 1] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_scan[0] = 0;
+      for (int bi = 0; bi < nbs; bi++) s_scan[bi + 1] += s_scan[bi];
     }
     __syncthreads();
 
-    const int nitems = (b1 - b0) * kt;
+    const int nitems = s_scan[nbs];
+    // Without r^2-type fits each thread takes a contiguous run of items (bra-major), so its bra
+    // polynomials change only when the run crosses a bra pair.  With them the items are dealt
+    // round-robin (consecutive threads, consecutive ket pairs of one bra pair): the threads of a
+    // warp then share their bra polynomials and the data-dependent branches of the option loops.
+    const int per_t = (nitems + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int e_begin = T2 ? (int)threadIdx.x : min(nitems, (int)threadIdx.x * per_t);
+    const int e_end = T2 ? nitems : min(nitems, e_begin + per_t);
+    const int e_step = T2 ? (int)blockDim.x : 1;
     int bcur = -1;
-    double Pn[3][NO][L + 1];
+    double Pn[3 * NO * (L + 1)];
     PrimPair P;
-    int ib = b0 + threadIdx.x / kt, ik = threadIdx.x % kt;  // item (bra, ket) of this thread
-    for (int e = threadIdx.x; e < nitems; e += blockDim.x) {
+    for (int e = e_begin; e < e_end; e += e_step) {
+      // item e -> (bra bi, ket ik): last bi with s_scan[bi] <= e
+      int lo = 0, hi = nbs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_scan[mid] <= e) lo = mid; else hi = mid - 1;
+      }
+      const int ib = b0 + lo, ik = self_out ? ib - t0 : e - s_scan[lo];
       if (ib != bcur) {
         P = bra[ib];
         bcur = ib;
-#pragma unroll
-        for (int ax = 0; ax < 3; ax++)
-#pragma unroll
-          for (int o = 0; o < NO; o++) {
-            if ((o & 1) && !t2[0]) continue;
-            if ((o & 2) && !t2[1]) continue;
-            pair_poly<L>(P.PA[ax], np[0][ax] + 2 * (o & 1), P.PB[ax], np[1][ax] + (o & 2), Pn[ax][o]);
-          }
+        pair_polys<L, T2>(S, 0, P, Pn);
       }
       const PrimPair& Q = s_ket[ik];
-      const double* Qn = s_q + (size_t)ik * QW;
-      const double p = P.p, qq = Q.p;
-      // src/general_primitive_integral.F90:54-60, 142-146
-      const double pq = P.p_inv * 0.5 * Q.p_inv;
-      const double rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
-      const double pq_inv = 0.5 * (rs_pq * rs_pq);
-      RecCoef R;
-      R.p10_1 = qq * pq;
-      R.p01_1 = p * pq;
-      const double pq_inv_2 = pq_inv + pq_inv;
-      R.p10_2 = pq_inv_2 * R.p10_1 * qq;
-      R.p01_2 = pq_inv_2 * R.p01_1 * p;
-      R.pq_inv = pq_inv;
-      const double rho = p * qq * pq_inv_2;
-      const double dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
-      const double T = (dx * dx + dy * dy + dz * dz) * rho;
-      double F[NF + 1];
-      boys_tab<NF>(T, nf, F, s_boys);
-
-      double accu;
-      if (!T2) {
-        double A[3][2 * L + 1];
-        int deg[3];
-#pragma unroll
-        for (int ax = 0; ax < 3; ax++) {
-          deg[ax] = amax[ax] + cmax[ax];
-          if (deg[ax] == 0) {
-            A[ax][0] = 1.0;
-#pragma unroll
-            for (int m = 1; m <= 2 * L; m++) A[ax][m] = 0.0;
-            continue;
-          }
-          double I[L + 1][L + 1][2 * L + 1];
-          const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
-          const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
-          rys_table<L>(R, Cc, Dd, amax[ax], cmax[ax], I);
-          axis_poly<L>(Pn[ax][0], amax[ax], Qn + ax * (L + 1), cmax[ax], I, ax == 0, A[ax]);
-        }
-        // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
-        double dp[4 * L + 1];
-#pragma unroll
-        for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
-#pragma unroll
-        for (int a = 0; a <= 2 * L; a++) {
-          if (a > deg[0]) break;
-#pragma unroll
-          for (int c = 0; c <= 2 * L; c++) {
-            if (c > deg[1]) break;
-            dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
-          }
-        }
-        double d1[NF + 1];
-#pragma unroll
-        for (int t = 0; t <= NF; t++) d1[t] = 0.0;
-#pragma unroll
-        for (int a = 0; a <= 4 * L; a++) {
-          if (a > deg[0] + deg[1] || a > NF) break;
-#pragma unroll
-          for (int c = 0; c <= 2 * L; c++) {
-            if (c > deg[2] || a + c > NF) break;
-            d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
-          }
-        }
-        accu = d1[0] * F[0];
-#pragma unroll
-        for (int n = 1; n <= NF; n++)
-          if (n <= nf) accu = fma(d1[n], F[n], accu);
-      } else {
-        // axis polynomials for every (bra option, ket option), then the cartesian combinations
-        double A[3][NO * NO][2 * L + 1];
-#pragma unroll 1
-        for (int ax = 0; ax < 3; ax++) {
-          double I[L + 1][L + 1][2 * L + 1];
-          const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
-          const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
-          rys_table<L>(R, Cc, Dd, amax[ax], cmax[ax], I);
-#pragma unroll 1
-          for (int ob = 0; ob < NO; ob++) {
-            if ((ob & 1) && !t2[0]) continue;
-            if ((ob & 2) && !t2[1]) continue;
-#pragma unroll 1
-            for (int oc = 0; oc < NO; oc++) {
-              if ((oc & 1) && !t2[2]) continue;
-              if ((oc & 2) && !t2[3]) continue;
-              const int da = np[0][ax] + np[1][ax] + 2 * (ob & 1) + (ob & 2);
-              const int dc = np[2][ax] + np[3][ax] + 2 * (oc & 1) + (oc & 2);
-              axis_poly<L>(Pn[ax][ob], da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0, A[ax][ob * NO + oc]);
-            }
-          }
-        }
-        accu = 0.0;
-        const int nci = t2[0] ? 3 : 1, nck = t2[1] ? 3 : 1, ncj = t2[2] ? 3 : 1, ncl = t2[3] ? 3 : 1;
-        for (int ci = 0; ci < nci; ci++)
-          for (int ck = 0; ck < nck; ck++)
-            for (int cj = 0; cj < ncj; cj++)
-              for (int cl = 0; cl < ncl; cl++) {
-                int sel[3], deg[3];
-#pragma unroll
-                for (int ax = 0; ax < 3; ax++) {
-                  const int ob = (t2[0] && ci == ax ? 1 : 0) | (t2[1] && ck == ax ? 2 : 0);
-                  const int oc = (t2[2] && cj == ax ? 1 : 0) | (t2[3] && cl == ax ? 2 : 0);
-                  sel[ax] = ob * NO + oc;
-                  deg[ax] = np[0][ax] + np[1][ax] + np[2][ax] + np[3][ax] + 2 * ((ob & 1) + (ob >> 1) + (oc & 1) + (oc >> 1));
-                }
-                const double* Ax = A[0][sel[0]];
-                const double* Ay = A[1][sel[1]];
-                const double* Az = A[2][sel[2]];
-                double dp[4 * L + 1];
-#pragma unroll
-                for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
-#pragma unroll
-                for (int a = 0; a <= 2 * L; a++) {
-                  if (a > deg[0]) break;
-#pragma unroll
-                  for (int c = 0; c <= 2 * L; c++) {
-                    if (c > deg[1]) break;
-                    dp[a + c] = fma(Ay[c], Ax[a], dp[a + c]);
-                  }
-                }
-                double d1[NF + 1];
-#pragma unroll
-                for (int t = 0; t <= NF; t++) d1[t] = 0.0;
-#pragma unroll
-                for (int a = 0; a <= 4 * L; a++) {
-                  if (a > deg[0] + deg[1] || a > NF) break;
-#pragma unroll
-                  for (int c = 0; c <= 2 * L; c++) {
-                    if (c > deg[2] || a + c > NF) break;
-                    d1[a + c] = fma(Az[c], dp[a], d1[a + c]);
-                  }
-                }
-                double s = d1[0] * F[0];
-#pragma unroll
-                for (int n = 1; n <= NF; n++)
-                  if (n <= nf) s = fma(d1[n], F[n], s);
-                accu = accu + s;
-              }
+      const double v = prim_quartet<L, T2>(S, P, Pn, Q, s_q + (size_t)ik * QW, s_boys);
+      if (self_out) {
+        self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
+        continue;
       }
-      // src/general_primitive_integral.F90:192 and the coefficient product of src/gauss_ijkl.F90:137
-      const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
-      acc = fma(P.coef * Q.coef, pref * accu, acc);
-      // next item of this thread
-      ik += blockDim.x;
-      while (ik >= kt) {
-        ik -= kt;
-        ib++;
-      }
+      // the coefficient product of src/gauss_ijkl.F90:137
+      acc = fma(P.coef * Q.coef, v, acc);
     }
   }
   // block reduction in a fixed order
@@ -416,6 +496,5 @@ __global__ void __launch_bounds__(128) eri_kernel(
   __syncthreads();
   if (threadIdx.x == 0) partial[w * split + part] = ((s_red[0] + s_red[1]) + s_red[2]) + s_red[3];
 }
-
 
 }  // namespace ss

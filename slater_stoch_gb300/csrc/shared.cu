@@ -84,56 +84,66 @@ __global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, Mi
   w[s] = isfinite(ww) ? (double)ww : 0.0;
 }
 
+// Fit residual of one shell as a function of t = sqrt(r): cubic Hermite table on a uniform grid
+// t_j = j h, j = 0..N, nodes (delta(t_j), h d(delta)/dt(t_j)), delta = u_orb - u_gauss.  Built in
+// FP64 on the host from the fit (build_resid_tables); beyond t_max both radial parts are below
+// e^-60 of their scale and the residual is u_orb.
+struct ResidDev {
+  const float2* node;   // all shells, concatenated
+  const int* off;       // first node of each shell (nshell + 1 entries)
+  const float* inv_h;   // 1/h per shell
+  const float* tmax;    // t_max per shell
+};
+
 // Orbital values at the samples (the factors of src/compute_densities.F90:51-53):
 // phiS_i = poly_i u_orb_i, phiG_i = poly_i u_gauss_i and the fit residual
-// delta_i = poly_i (u_orb_i - u_gauss_i).  With 20-Gaussian fits delta/phi is 1e-5..1e-8, so the
-// residual is formed in FP64 (a difference of two FP32 values would be rounding noise); Gaussian
-// terms whose exponent exceeds the most diffuse term's by more than 60 (relative size < 1e-26
-// times a coefficient ratio) are skipped.  The radial parts are evaluated once per shell (the
-// consecutive functions sharing centre, STO exponent and fit, which differ only by their
-// cartesian monomial).  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
+// delta_i = poly_i (u_orb_i - u_gauss_i).  With 20-Gaussian fits delta/phi is 1e-5..1e-8; the
+// residual comes from its FP64-built table (interpolation error below 1e-6 of the shell's largest
+// residual), so the whole evaluation runs in FP32: u_orb = r^n_sto e^(-zeta r), u_gauss = u_orb -
+// delta.  One block row per shell (consecutive functions sharing centre, STO exponent and fit,
+// which differ only by their cartesian monomial).  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
 __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, const int* __restrict__ shell_start,
-                                         const double* __restrict__ u1, const double* __restrict__ u2,
-                                         float* __restrict__ out) {
+                                         ResidDev R, const double* __restrict__ u1,
+                                         const double* __restrict__ u2, float* __restrict__ out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int sh = blockIdx.y;
   if (s >= S) return;
   const int i = shell_start[sh], i_end = shell_start[sh + 1];
   const double* A = B.center + 3 * i;
   const int nsto = B.n_sto[i];
-  const double zeta = B.g_slater[i];
-  const int ng = B.n_gauss[i];
-  const double* c1 = B.c_gauss + (int64_t)B.ld * i;
-  const double* c2 = B.c_gauss + (int64_t)B.ld * (i + (int64_t)B.n);
-  const double* gg = B.g_gauss + (int64_t)B.ld * i;
-  float gmin = 3.0e38f;
-  for (int m = 0; m < ng; m++) gmin = fminf(gmin, (float)gg[m]);
+  const float zeta = (float)B.g_slater[i];
+  const float2* tab = R.node + R.off[sh];
+  const int nint = R.off[sh + 1] - R.off[sh] - 1;
+  const float inv_h = R.inv_h[sh], tmax = R.tmax[sh];
   const int64_t plane = (int64_t)B.n * ld;
 #pragma unroll
   for (int e = 0; e < 2; e++) {
     const double* u = e == 0 ? u1 : u2;
-    const double dx = u[3 * s] - A[0], dy = u[3 * s + 1] - A[1], dz = u[3 * s + 2] - A[2];
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    const double r = sqrt(r2);
-    double uo = exp(-zeta * r);
+    const float dx = (float)(u[3 * s] - A[0]), dy = (float)(u[3 * s + 1] - A[1]), dz = (float)(u[3 * s + 2] - A[2]);
+    const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    float uo = expf(-zeta * r);
     for (int t = 0; t < nsto; t++) uo *= r;
-    const float r2f = (float)r2;
-    const float ycut = gmin * r2f + 60.0f;
-    double ug = 0.0;
-    for (int m = 0; m < ng; m++) {
-      if ((float)gg[m] * r2f > ycut) continue;
-      ug += (c1[m] + c2[m] * r2) * exp(-gg[m] * r2);
+    const float t = sqrtf(r);
+    float res = uo;
+    if (t < tmax) {
+      const float x = t * inv_h;
+      const int j = min((int)x, nint - 1);
+      const float v = x - (float)j;
+      const float2 a = tab[j], b = tab[j + 1];
+      const float v2 = v * v, v3 = v2 * v;
+      res = fmaf(2.f * v3 - 3.f * v2 + 1.f, a.x,
+                 fmaf(v3 - 2.f * v2 + v, a.y, fmaf(3.f * v2 - 2.f * v3, b.x, (v3 - v2) * b.y)));
     }
-    const double res = uo - ug;
+    const float ug = uo - res;
     for (int f = i; f < i_end; f++) {
-      double poly = 1.0;
-      for (int t = 0; t < B.npower[3 * f]; t++) poly *= dx;
-      for (int t = 0; t < B.npower[3 * f + 1]; t++) poly *= dy;
-      for (int t = 0; t < B.npower[3 * f + 2]; t++) poly *= dz;
+      float poly = 1.f;
+      for (int t2 = 0; t2 < B.npower[3 * f]; t2++) poly *= dx;
+      for (int t2 = 0; t2 < B.npower[3 * f + 1]; t2++) poly *= dy;
+      for (int t2 = 0; t2 < B.npower[3 * f + 2]; t2++) poly *= dz;
       const int64_t o = (int64_t)f * ld + s;
-      out[(3 * e) * plane + o] = (float)(poly * uo);
-      out[(3 * e + 1) * plane + o] = (float)(poly * ug);
-      out[(3 * e + 2) * plane + o] = (float)(poly * res);
+      out[(3 * e) * plane + o] = poly * uo;
+      out[(3 * e + 1) * plane + o] = poly * ug;
+      out[(3 * e + 2) * plane + o] = poly * res;
     }
   }
 }
@@ -227,6 +237,7 @@ struct SharedPlan {
   std::vector<int> shell_start;     // consecutive functions with identical radial part
   int* d_shell = nullptr;
   MixDev mix{};
+  ResidDev resid{};
 };
 
 static bool same_radial(const ss_ctx* c, int a, int b) {
@@ -242,6 +253,99 @@ static bool same_radial(const ss_ctx* c, int a, int b) {
       if (c->h_cg[m + ld * (a + n * t)] != c->h_cg[m + ld * (b + n * t)]) return false;
   }
   return true;
+}
+
+// Residual tables of the shells (cached per basis): for each shell a cubic Hermite table of
+// delta(t) = u_orb - u_gauss on t = sqrt(r) in [0, t_max], r_max = max(60/zeta, sqrt(60/g_min)),
+// built in FP64.  N starts at 4096 intervals and doubles until the error at every interval
+// midpoint (with the FP32-rounded nodes) is below 1e-6 of the shell's largest |delta|.
+static int build_resid_tables(ss_ctx* c, const std::vector<int>& shell_start, ResidDev* out) {
+  const int n = c->n, ld = c->ld;
+  const int nsh = (int)shell_start.size() - 1;
+  if (!c->have_resid) {
+    std::vector<float2> node;
+    std::vector<int> off(nsh + 1, 0);
+    std::vector<float> invh(nsh), tmax(nsh);
+    for (int sh = 0; sh < nsh; sh++) {
+      const int f = shell_start[sh];
+      const double zeta = c->h_gs[f];
+      const int k = c->h_nsto[f], ng = c->h_ng[f];
+      const double* c1 = &c->h_cg[(size_t)ld * f];
+      const double* c2 = &c->h_cg[(size_t)ld * (f + n)];
+      const double* g = &c->h_gg[(size_t)ld * f];
+      double gmin = 1e300;
+      for (int m = 0; m < ng; m++) gmin = std::min(gmin, g[m]);
+      const double rmax = std::max(60.0 / zeta, ng > 0 ? sqrt(60.0 / gmin) : 0.0);
+      const double tm = sqrt(rmax);
+      auto eval = [&](double r, double* d, double* dd) {  // delta and d(delta)/dr
+        const double ez = exp(-zeta * r);
+        double rk = 1.0, rk1 = 0.0;  // r^k, k r^(k-1)
+        for (int t = 0; t < k; t++) {
+          rk1 = rk1 * r + rk;
+          rk *= r;
+        }
+        double ug = 0.0, dug = 0.0;
+        for (int m = 0; m < ng; m++) {
+          const double eg = exp(-g[m] * r * r);
+          const double poly = c1[m] + c2[m] * r * r;
+          ug += poly * eg;
+          dug += (2.0 * c2[m] * r - 2.0 * g[m] * r * poly) * eg;
+        }
+        *d = rk * ez - ug;
+        *dd = (rk1 - zeta * rk) * ez - dug;
+      };
+      std::vector<float2> tab;
+      double h = 0.0;
+      for (int N = 4096;; N *= 2) {
+        h = tm / N;
+        tab.resize(N + 1);
+        double dmax = 0.0;
+        for (int j = 0; j <= N; j++) {
+          const double t = j * h;
+          double d, dd;
+          eval(t * t, &d, &dd);
+          tab[j] = make_float2((float)d, (float)(h * 2.0 * t * dd));
+          dmax = std::max(dmax, fabs(d));
+        }
+        double emax = 0.0;
+        for (int j = 0; j < N; j++) {
+          const double t = (j + 0.5) * h;
+          double d, dd;
+          eval(t * t, &d, &dd);
+          const double interp = 0.5 * ((double)tab[j].x + (double)tab[j + 1].x) +
+                                0.125 * ((double)tab[j].y - (double)tab[j + 1].y);
+          emax = std::max(emax, fabs(interp - d));
+        }
+        if (emax <= 1e-6 * dmax || dmax == 0.0) break;
+        if (N >= 65536) {
+          ss_set_error_msg("shared estimator: the fit residual of function %d is not resolved by a "
+                           "65536-interval table (error %.3g of its maximum)", f + 1, emax / dmax);
+          return SS_ERR_UNSUPPORTED;
+        }
+      }
+      off[sh] = (int)node.size();
+      node.insert(node.end(), tab.begin(), tab.end());
+      invh[sh] = (float)(1.0 / h);
+      tmax[sh] = (float)tm;
+    }
+    off[nsh] = (int)node.size();
+    float2* dn;
+    int* doff;
+    float *dih, *dtm;
+    TRY(upload_v(c, "rs_node", node, &dn));
+    TRY(upload_v(c, "rs_off", off, &doff));
+    TRY(upload_v(c, "rs_invh", invh, &dih));
+    TRY(upload_v(c, "rs_tmax", tmax, &dtm));
+    c->have_resid = true;
+  }
+  void* p;
+  ResidDev R;
+  TRY(pool_get(c, "rs_node", 0, &p)); R.node = (const float2*)p;
+  TRY(pool_get(c, "rs_off", 0, &p)); R.off = (const int*)p;
+  TRY(pool_get(c, "rs_invh", 0, &p)); R.inv_h = (const float*)p;
+  TRY(pool_get(c, "rs_tmax", 0, &p)); R.tmax = (const float*)p;
+  *out = R;
+  return SS_OK;
 }
 
 static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
@@ -307,6 +411,7 @@ static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
     if (!same_radial(c, f, S.shell_start.back())) S.shell_start.push_back(f);
   S.shell_start.push_back(c->n);
   TRY(upload_v(c, "sh_shell", S.shell_start, &S.d_shell));
+  TRY(build_resid_tables(c, S.shell_start, &S.resid));
   return SS_OK;
 }
 
@@ -362,7 +467,7 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
       shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, u1, u2, w);
       SS_CUDA_TRY(cudaGetLastError());
       shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)(SP.shell_start.size() - 1)), 128, 0,
-                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, u1, u2, F);
+                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, SP.resid, u1, u2, F);
       SS_CUDA_TRY(cudaGetLastError());
       shared_operand_kernel<<<dim3((unsigned)((Kh + 255) / 256), (unsigned)P), 256, 0, c->stream>>>(
           ns, Kh, Sc, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);

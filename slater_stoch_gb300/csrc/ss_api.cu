@@ -1,6 +1,7 @@
 // ss_api.cu -- context, basis/quartet setup and the analytic-ERI entry points of the C ABI.
 #include <math.h>
 #include <stdarg.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -18,8 +19,11 @@ void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem);
 cudaError_t launch_eri_class(int L, bool t2, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
-                             const int32_t* ks, const int32_t* ls, double* partial);
+                             const int32_t* ks, const int32_t* ls, const double* pre, double eps,
+                             double* partial, double* self_out);
+__global__ void prim_pair_sort(const PrimPair* in, const int64_t* off, const int* cnt, PrimPair* out);
 __global__ void prim_pair_count(BasisDev B, int npairs, int* cnt);
+void jobs_shutdown(ss_ctx* c);
 __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* off, PrimPair* out);
 __global__ void eri_finalize(int64_t nint, const int32_t* is, const int32_t* js, const int32_t* ks,
                              const int32_t* ls, const int64_t* slot, int split, const double* partial,
@@ -121,7 +125,8 @@ static int total_pow(const ss_ctx* c, int f) {
 static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const int32_t* d_qks,
                    const int32_t* d_qls, const std::vector<int32_t>& qis, const std::vector<int32_t>& qjs,
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
-                   const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out) {
+                   const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out,
+                   const double* d_pre, double eps, double* self_out = nullptr) {
   // bucket by class (L = max(bra L, ket L), any r^2-type fit among the four functions)
   const int NB = 2 * (SS_MAX_POW + 1);
   std::vector<std::vector<int64_t>> bucket(NB);
@@ -132,8 +137,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     bucket[2 * L + (t2 ? 1 : 0)].push_back(t);
   }
   int64_t nsel = (int64_t)sel.size();
-  // one split for all classes keeps the slot arithmetic simple
-  const int target = c->num_sms * 8;
+  // one split for all classes keeps the slot arithmetic simple; short lists (the Schwarz
+  // diagonal: n(n+1)/2 quartets, a few of them in each heavy class) are split up to 16 ways
+  const int target = c->num_sms * 32;
   int split = (int)std::min<int64_t>(16, std::max<int64_t>(1, (target + std::max<int64_t>(nsel, 1) - 1) /
                                                              std::max<int64_t>(nsel, 1)));
   split_out = split;
@@ -173,7 +179,8 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
       cudaError_t e = launch_eri_class(L, t2, grid, ktile, smem, c->stream, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
-                                       d_qjs, d_qks, d_qls, d_partial + (begin[bk] + s0) * split);
+                                       d_qjs, d_qks, d_qls, d_pre, eps, d_partial + (begin[bk] + s0) * split,
+                                       self_out);
       if (e != cudaSuccess) {
         ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
         return SS_ERR_CUDA;
@@ -189,6 +196,27 @@ int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out) {
   int rc = dev_alloc(c, b, bytes);
   if (rc) return rc;
   *out = b.ptr;
+  return SS_OK;
+}
+
+#define TRY(x)           \
+  do {                   \
+    int rc_ = (x);       \
+    if (rc_) return rc_; \
+  } while (0)
+
+// Sort the primitive pairs of every function pair by decreasing Schwarz factor (the order the
+// primitive screening of the ERI kernel relies on).
+static int sort_prim_pairs(ss_ctx* c) {
+  const int npairs = c->n * (c->n + 1) / 2;
+  const size_t bytes = sizeof(PrimPair) * std::max<int64_t>(c->h_pp_off[npairs], 1);
+  void* p;
+  TRY(pool_get(c, "pp_sorted", bytes, &p));
+  prim_pair_sort<<<npairs, 512, 0, c->stream>>>((const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
+                                                 (const int*)c->d_pp_cnt.ptr, (PrimPair*)p);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  SS_CUDA_TRY(cudaMemcpyAsync(c->d_pp.ptr, p, bytes, cudaMemcpyDeviceToDevice, c->stream));
   return SS_OK;
 }
 
@@ -214,9 +242,16 @@ int ensure_precond(ss_ctx* c) {
   std::vector<int64_t> sel(np), slot;
   std::iota(sel.begin(), sel.end(), 0);
   int split = 1;
+  // 1. primitive-pair Schwarz factors (items (P,P) of the diagonal quartets) into pad[0],
+  // 2. per-pair sort by decreasing factor, 3. the diagonal quartets themselves
   if (!rc)
     rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
-                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split);
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split, nullptr, 0.0,
+                 (double*)((char*)c->d_pp.ptr + offsetof(PrimPair, pad)));
+  if (!rc) rc = sort_prim_pairs(c);
+  if (!rc)
+    rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split, nullptr, 0.0);
   if (rc) {
     dev_free(c, di);
     dev_free(c, dk);
@@ -275,7 +310,8 @@ int ensure_gauss(ss_ctx* c) {
   std::vector<int64_t> slot;
   int split = 1;
   rc = run_eri(c, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
-               (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, split);
+               (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, split,
+               (const double*)c->d_precond.ptr, PRIM_SCREEN_EPS);
   if (rc) return rc;
   rc = h2d(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
   if (rc) return rc;
@@ -346,6 +382,7 @@ ss_ctx* ss_create(int device, size_t hbm_budget) {
 
 void ss_destroy(ss_ctx* c) {
   if (!c) return;
+  jobs_shutdown(c);
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->d_center, &c->d_npower, &c->d_nsto, &c->d_itype, &c->d_ng, &c->d_cg, &c->d_gg,
@@ -447,6 +484,7 @@ int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower,
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;
   c->have_precond = c->have_gauss = c->have_mc = false;
+  c->have_resid = false;
   return SS_OK;
 }
 

@@ -23,6 +23,11 @@ namespace ss {
 constexpr int SS_MAX_POW = 4;        // per-function per-axis power, incl. the +2 of r^2 fits
 constexpr int SS_MAX_NG = 30;        // Gaussians per fit (src/common_data.F90:7)
 constexpr int SS_MAX_NF = 24;        // highest Boys order F_n used by one primitive quartet
+// Primitive screening of the analytic ERIs: a primitive quartet whose Schwarz bound S_P S_Q is
+// below PRIM_SCREEN_EPS * sqrt((ik|ik)(jl|jl)) is skipped.  With at most 30 x 30 primitive pairs
+// per function pair the skipped part of an ERI is below 8.1e5 * 1e-18 = 8.1e-13 of its Schwarz
+// bound sqrt((ik|ik)(jl|jl)), and in practice far below (the bound is loose, the signs vary).
+constexpr double PRIM_SCREEN_EPS = 1e-18;
 
 // One primitive pair of a function pair (i,k): the Gaussian product of
 // g_gauss(m1,i) and g_gauss(m2,k) (src/gaussian_product.F90:1-33), padded to 128 bytes.
@@ -33,8 +38,9 @@ struct __align__(16) PrimPair {
   double coef;           // c(m1,i) * c(m2,k)
   double PA[3];          // P - A  (pows_a(1) of src/give_explicit_poly_and_gaussian.F90:125)
   double PB[3];          // P - B
-  double pad[3];
+  double pad[3];         // [0] Schwarz factor sqrt(coef^2 (P|P)), [1] index m1*ng(k)+m2, [2] unused
 };
+static_assert(sizeof(PrimPair) == 16 * sizeof(double), "PrimPair is 16 doubles (the kernels stride by 16)");
 
 // Device view of the fitted basis (Fortran layouts, 0-based).
 struct BasisDev {

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,10 @@ struct Mixture {
 
 }  // namespace ss
 
+namespace ss {
+struct JobState;  // jobs.cu
+}
+
 struct ss_ctx {
   int device = 0;
   size_t budget = 0, used = 0;
@@ -70,6 +75,11 @@ struct ss_ctx {
 
   // MC results
   bool have_mc = false;
+  bool have_resid = false;  // shared-walker residual tables of the current basis (pool "rs_*")
+
+  // asynchronous jobs (jobs.cu)
+  std::map<int64_t, std::shared_ptr<ss::JobState>> jobs;
+  int64_t next_job = 1;
   ss::DevBuf d_mean, d_sigma;
 
   // scratch reused across calls
