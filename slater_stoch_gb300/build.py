@@ -51,7 +51,7 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     OUTDIR.mkdir(parents=True, exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu"))
     extra = list(extra or [])
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 8, len(srcs)))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     newest = max(o.stat().st_mtime for o in objs)
     if LIB.exists() and LIB.stat().st_mtime >= newest:

@@ -163,28 +163,44 @@ void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
   *smem = per * kt;
 }
 
-cudaError_t launch_eri_L0n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L1n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L2n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L3n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4n(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L2t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L3t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4t(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L0c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L1c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L2c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L3c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L2c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L3c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L2c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
 
-cudaError_t launch_eri_class(int L, bool t2, dim3 grid, int ktile, size_t smem, cudaStream_t st,
+// Kernel instance for class (L, tc).  tc: number of r^2-type fits among the four functions
+// (0, 1, 2, 3 = three or four).  A quartet with r^2-type fits has L >= 2, and one with three or
+// four has L = 4; an instance with a larger L serves any smaller one (degrees are runtime).
+cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
                              double* partial, double* self_out) {
-  if (L == 0 && t2 == false) return launch_eri_L0n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 1 && t2 == false) return launch_eri_L1n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 2 && t2 == false) return launch_eri_L2n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 3 && t2 == false) return launch_eri_L3n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 4 && t2 == false) return launch_eri_L4n(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 2 && t2 == true) return launch_eri_L2t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 3 && t2 == true) return launch_eri_L3t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-  if (L == 4 && t2 == true) return launch_eri_L4t(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  if (tc == 0) {
+    if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 2) return launch_eri_L2c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 3) return launch_eri_L3c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 4) return launch_eri_L4c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  } else if (tc == 1) {
+    if (L <= 2) return launch_eri_L2c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 3) return launch_eri_L3c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 4) return launch_eri_L4c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  } else if (tc == 2) {
+    if (L <= 2) return launch_eri_L2c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 3) return launch_eri_L3c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 4) return launch_eri_L4c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  } else if (tc == 3) {
+    if (L <= 4) return launch_eri_L4c3(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+  }
   return cudaErrorInvalidValue;
 }
 

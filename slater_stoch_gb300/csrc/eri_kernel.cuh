@@ -169,6 +169,7 @@ struct QuartetShape {
   int t2[4];
   int nf;
   int amax[3], cmax[3];
+  int nt, tf[4];  // number and positions (0..3 = i, k, j, l) of the r^2-type fits
 };
 
 template <bool T2>
@@ -191,7 +192,25 @@ __device__ __forceinline__ QuartetShape quartet_shape(const BasisDev& B, int fi,
     S.amax[ax] = S.np[0][ax] + S.np[1][ax] + 2 * (S.t2[0] + S.t2[1]);
     S.cmax[ax] = S.np[2][ax] + S.np[3][ax] + 2 * (S.t2[2] + S.t2[3]);
   }
+  S.nt = 0;
+#pragma unroll
+  for (int f = 0; f < 4; f++) {
+    S.tf[f] = 0;
+    if (S.t2[f]) S.tf[S.nt++] = f;
+  }
   return S;
+}
+
+// Which functions of the quartet take the +2 of their r^2 fit on one axis, for a subset s of
+// the r^2-type functions (bit b of s = function tf[b]): bra option ob (bit0 = i, bit1 = k), ket
+// option oc (bit0 = j, bit1 = l), as used by pair_polys.
+__device__ __forceinline__ void subset_options(const QuartetShape& S, int s, int& ob, int& oc) {
+  int plus[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int b = 0; b < 4; b++)
+    if (b < S.nt && ((s >> b) & 1)) plus[S.tf[b]] = 1;
+  ob = plus[0] | (plus[1] << 1);
+  oc = plus[2] | (plus[3] << 1);
 }
 
 // recentred pair polynomials of a primitive pair, per (axis, option); side 0 = bra (functions
@@ -214,9 +233,12 @@ __device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, cons
 // One primitive quartet (src/general_primitive_integral.F90, summed over the cartesian
 // components of the r^2-type fits): returns pref * sum_n d1[n] F_n; the caller multiplies by
 // the coefficient product P.coef * Q.coef.  Pn, Qn: pair_polys of the bra and ket pairs.
-template <int L, bool T2>
+// TC: 0 = no r^2-type fit; 1, 2 = exactly one / two of them (subset recursion over the axes,
+// below); 3 = three or four (all cartesian combinations enumerated).
+template <int L, int TC>
 __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const PrimPair& P, const double* Pn,
                                                const PrimPair& Q, const double* Qn, const double* s_boys) {
+  constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;
   constexpr int NF = (6 * L < 16) ? 6 * L : 16;
   const double p = P.p, qq = Q.p;
@@ -286,6 +308,76 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
 #pragma unroll
     for (int n = 1; n <= NF; n++)
       if (n <= nf) accu = fma(d1[n], F[n], accu);
+  } else if (TC == 1 || TC == 2) {
+    // With t = TC r^2-type fits, a cartesian combination assigns each fit's +2 to one axis, i.e.
+    // splits the set of fits into (Sx, Sy, Sz).  sum over combinations of L(Ax[Sx] Ay[Sy] Az[Sz])
+    // is built axis by axis: Qxy[S] = sum_{Sx subset S} Ax[Sx] Ay[S \ Sx], then
+    // sum_Sz L(Qxy[all \ Sz] Az[Sz]), L(p) = sum_n p[n] F_n.  Same per-axis polynomials (and
+    // thresholds) as the enumeration of the 3^t combinations, 2^t final contractions instead of 3^t.
+    constexpr int NS = 1 << (TC == 1 ? 1 : 2);
+    double Ax[NS][2 * L + 1], Qxy[NS][4 * L + 1];
+    int dAx[NS], dQ[NS];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      double I[L + 1][L + 1][2 * L + 1];
+      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
+      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
+      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      if (ax == 1) {
+#pragma unroll
+        for (int t = 0; t < NS; t++) {
+          dQ[t] = -1;
+#pragma unroll
+          for (int m = 0; m <= 4 * L; m++) Qxy[t][m] = 0.0;
+        }
+      }
+#pragma unroll
+      for (int sa = 0; sa < NS; sa++) {
+        int ob, oc;
+        subset_options(S, sa, ob, oc);
+        const int da = S.np[0][ax] + S.np[1][ax] + 2 * (ob & 1) + (ob & 2);
+        const int dc = S.np[2][ax] + S.np[3][ax] + 2 * (oc & 1) + (oc & 2);
+        double Aa[2 * L + 1];
+        axis_poly<L>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0, Aa);
+        const int dA = da + dc;
+        if (ax == 0) {
+#pragma unroll
+          for (int m = 0; m <= 2 * L; m++) Ax[sa][m] = Aa[m];
+          dAx[sa] = dA;
+        } else if (ax == 1) {
+#pragma unroll
+          for (int sx = 0; sx < NS; sx++) {
+            if (sx & sa) continue;
+            const int st = sx | sa;
+            dQ[st] = max(dQ[st], dAx[sx] + dA);
+#pragma unroll
+            for (int a = 0; a <= 2 * L; a++) {
+              if (a > dAx[sx]) break;
+#pragma unroll
+              for (int c = 0; c <= 2 * L; c++) {
+                if (c > dA) break;
+                Qxy[st][a + c] = fma(Aa[c], Ax[sx][a], Qxy[st][a + c]);
+              }
+            }
+          }
+        } else {
+          const int st = (NS - 1) ^ sa;
+          double sum = 0.0;
+#pragma unroll
+          for (int c = 0; c <= 2 * L; c++) {
+            if (c > dA) break;
+            double g = 0.0;
+#pragma unroll
+            for (int a = 0; a <= 4 * L; a++) {
+              if (a > dQ[st] || a + c > NF) break;
+              g = fma(Qxy[st][a], F[a + c], g);
+            }
+            sum = fma(Aa[c], g, sum);
+          }
+          accu = (sa == 0) ? sum : accu + sum;
+        }
+      }
+    }
   } else {
     // axis polynomials for every (bra option, ket option), then the cartesian combinations
     double A[3][NO * NO][2 * L + 1];
@@ -381,14 +473,16 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
 // distribution (summed over the cartesian components of r^2-type fits) times its coefficient,
 // is written to self_out[16 * (pair_off + P)] (PrimPair::pad[0] of the pair).  By
 // Cauchy-Schwarz |c_P c_Q (P|Q)| <= S_P S_Q for every primitive quartet.
-// T2: some of the four functions are r^2-type fits (3 cartesian components sharing exponents).
-template <int L, bool T2>
+// TC: how many of the four functions are r^2-type fits (3 cartesian components sharing
+// exponents): 0, 1, 2, or 3 for three or four.
+template <int L, int TC>
 __global__ void __launch_bounds__(128) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
     const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
     const int32_t* __restrict__ ls, const double* __restrict__ pre, double eps, double* __restrict__ partial,
     double* __restrict__ self_out) {
+  constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
   constexpr int QW = 3 * NO * (L + 1);  // ket polynomial doubles per ket pair
   extern __shared__ double2 s_raw[];
@@ -480,7 +574,7 @@ __global__ void __launch_bounds__(128) eri_kernel(
         pair_polys<L, T2>(S, 0, P, Pn);
       }
       const PrimPair& Q = s_ket[ik];
-      const double v = prim_quartet<L, T2>(S, P, Pn, Q, s_q + (size_t)ik * QW, s_boys);
+      const double v = prim_quartet<L, TC>(S, P, Pn, Q, s_q + (size_t)ik * QW, s_boys);
       if (self_out) {
         self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
         continue;

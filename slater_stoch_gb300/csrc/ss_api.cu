@@ -16,7 +16,7 @@
 namespace ss {
 cudaError_t eri_init_constants();
 void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem);
-cudaError_t launch_eri_class(int L, bool t2, dim3 grid, int ktile, size_t smem, cudaStream_t st,
+cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
@@ -127,14 +127,15 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out,
                    const double* d_pre, double eps, double* self_out = nullptr) {
-  // bucket by class (L = max(bra L, ket L), any r^2-type fit among the four functions)
-  const int NB = 2 * (SS_MAX_POW + 1);
+  // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
+  // functions, 3 standing for three or four)
+  const int NB = 4 * (SS_MAX_POW + 1);
   std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
     int i = qis[t] - 1, k = qks[t] - 1, j = qjs[t] - 1, l = qls[t] - 1;
     int L = std::max(pair_L(c, i, k), pair_L(c, j, l));
-    bool t2 = c->h_itype[i] == 2 || c->h_itype[k] == 2 || c->h_itype[j] == 2 || c->h_itype[l] == 2;
-    bucket[2 * L + (t2 ? 1 : 0)].push_back(t);
+    int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
+    bucket[4 * L + std::min(nt, 3)].push_back(t);
   }
   int64_t nsel = (int64_t)sel.size();
   // one split for all classes keeps the slot arithmetic simple; short lists (the Schwarz
@@ -166,8 +167,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   double* d_partial = (double*)c->d_scratch_b.ptr;
   for (int bk = 0; bk < NB; bk++) {
     if (!count[bk]) continue;
-    const int L = bk / 2;
-    const bool t2 = bk & 1;
+    const int L = bk / 4;
+    const int tc = bk % 4;
+    const bool t2 = tc > 0;
     int ktile;
     size_t smem;
     eri_tile(L, t2, std::max(maxk[bk], 1), &ktile, &smem);
@@ -176,7 +178,7 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     for (int64_t s0 = 0; s0 < count[bk]; s0 += chunk) {
       int64_t nq = std::min(chunk, count[bk] - s0);
       dim3 grid((unsigned)(nq * split));
-      cudaError_t e = launch_eri_class(L, t2, grid, ktile, smem, c->stream, c->basis,
+      cudaError_t e = launch_eri_class(L, tc, grid, ktile, smem, c->stream, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
                                        d_qjs, d_qks, d_qls, d_pre, eps, d_partial + (begin[bk] + s0) * split,
