@@ -129,6 +129,51 @@ __device__ __forceinline__ void rys_table(const RecCoef& R, double Cc, double Dd
   }
 }
 
+// The same table when bra and ket share one centre (all four functions on one atom): C00 and
+// D00 vanish, so only the B10/B01/B00 terms remain and every entry with a + c odd is zero.
+template <int L>
+__device__ __forceinline__ void rys_table_1c(const RecCoef& R, int amax, int cmax,
+                                             double (&I)[L + 1][L + 1][2 * L + 1]) {
+#pragma unroll
+  for (int c = 0; c <= L; c++) {
+    if (c > cmax) break;
+#pragma unroll
+    for (int m = 0; m <= 2 * L; m++) {
+      if (m > c) break;
+      double v = 0.0;
+      if (c == 0) {
+        v = 1.0;
+      } else if (!(c & 1) && c >= 2) {
+        if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (double)(c - 1));
+        if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (double)(c - 1));
+      }
+      I[0][c][m] = v;
+    }
+  }
+#pragma unroll
+  for (int a = 1; a <= L; a++) {
+    if (a > amax) break;
+#pragma unroll
+    for (int c = 0; c <= L; c++) {
+      if (c > cmax) break;
+#pragma unroll
+      for (int m = 0; m <= 2 * L; m++) {
+        if (m > a + c) break;
+        double v = 0.0;
+        if (!((a + c) & 1)) {
+          if (a >= 2) {
+            const double s = (double)(a - 1);
+            if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
+            if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
+          }
+          if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (double)c);
+        }
+        I[a][c][m] = v;
+      }
+    }
+  }
+}
+
 // |x| < t and |x| > t on the bit patterns (integer pipe; x finite, t > 0)
 __device__ __forceinline__ bool abs_lt(double x, double t) {
   return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(t);
@@ -170,6 +215,7 @@ struct QuartetShape {
   int nf;
   int amax[3], cmax[3];
   int nt, tf[4];  // number and positions (0..3 = i, k, j, l) of the r^2-type fits
+  int onec;       // all four functions on one centre
 };
 
 template <bool T2>
@@ -198,6 +244,12 @@ __device__ __forceinline__ QuartetShape quartet_shape(const BasisDev& B, int fi,
     S.tf[f] = 0;
     if (S.t2[f]) S.tf[S.nt++] = f;
   }
+  S.onec = 1;
+#pragma unroll
+  for (int f = 1; f < 4; f++)
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++)
+      if (B.center[3 * fn[f] + ax] != B.center[3 * fn[0] + ax]) S.onec = 0;
   return S;
 }
 
@@ -276,7 +328,8 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
       double I[L + 1][L + 1][2 * L + 1];
       const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
       const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
-      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
+      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       axis_poly<L>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (L + 1), S.cmax[ax], I, ax == 0, A[ax]);
     }
     // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
@@ -322,7 +375,8 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
       double I[L + 1][L + 1][2 * L + 1];
       const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
       const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
-      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
+      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       if (ax == 1) {
 #pragma unroll
         for (int t = 0; t < NS; t++) {
@@ -386,7 +440,8 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
       double I[L + 1][L + 1][2 * L + 1];
       const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
       const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
-      rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
+      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
 #pragma unroll 1
       for (int ob = 0; ob < NO; ob++) {
         if ((ob & 1) && !S.t2[0]) continue;

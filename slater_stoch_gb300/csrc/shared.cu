@@ -18,69 +18,72 @@ namespace ss {
 
 struct MixDev {
   int m;
-  const double* G;      // [3m]
-  const double* c;      // [m]
-  const double* cdf;    // [m], cdf[m-1] == 1
-  const float* Gf;      // [3m]
+  const double* G;      // [3m] component centres
+  const float* Gf;      // [3m] centres rounded to float (hi part)
+  const float* Glo;     // [3m] G - Gf (lo part)
+  const float* cf;      // [m] ZV-map scale c of each component
   const float* inv2c;   // 1/(2c)
   const float* norm;    // w_c / ((2 pi)^{3/2} 2 c^{3/2})
 };
 
-__device__ __forceinline__ int pick_component(const MixDev& M, double u) {
-  int lo = 0, hi = M.m - 1;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (u <= M.cdf[mid]) hi = mid; else lo = mid + 1;
-  }
-  return lo;
+// standard normal from one 32-bit word: bit 0 the sign, bits 1..31 the tail probability
+// p in (0, 1/2) (|x| up to 6.2)
+__device__ __forceinline__ float normal_from_word(uint32_t w) {
+  const float p = ((float)(w >> 1) + 0.5f) * 2.3283064365386963e-10f;  // 2^-32
+  const float x = normcdfinvf(p);                                      // <= 0
+  return (w & 1u) ? x : -x;
 }
 
-// mixture density pi(u) = sum_c norm_c exp(-|u-G_c|/(2c)) |u-G_c|^{-3/2}
-__device__ __forceinline__ float mixture_density(const MixDev& M, const double (&u)[3]) {
+// mixture density pi(u) = sum_c norm_c exp(-|u-G_c|/(2c)) |u-G_c|^{-3/2} at u = G_d + off, in
+// FP32: u - G_c = (Gf_d - Gf_c) + ((Glo_d - Glo_c) + off), exact where G_c == G_d and within
+// ~1e-7 bohr elsewhere
+__device__ __forceinline__ float mixture_density(const MixDev& M, int d, const float (&off)[3]) {
+  const float h0 = M.Gf[3 * d], h1 = M.Gf[3 * d + 1], h2 = M.Gf[3 * d + 2];
+  const float l0 = M.Glo[3 * d], l1 = M.Glo[3 * d + 1], l2 = M.Glo[3 * d + 2];
   float tot = 0.f;
   for (int c = 0; c < M.m; c++) {
-    float dx = (float)(u[0] - M.G[3 * c]), dy = (float)(u[1] - M.G[3 * c + 1]), dz = (float)(u[2] - M.G[3 * c + 2]);
-    float rho = sqrtf(dx * dx + dy * dy + dz * dz);
-    float ir = rsqrtf(rho);
+    const float dx = (h0 - M.Gf[3 * c]) + ((l0 - M.Glo[3 * c]) + off[0]);
+    const float dy = (h1 - M.Gf[3 * c + 1]) + ((l1 - M.Glo[3 * c + 1]) + off[1]);
+    const float dz = (h2 - M.Gf[3 * c + 2]) + ((l2 - M.Glo[3 * c + 2]) + off[2]);
+    const float rho = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    const float ir = rsqrtf(rho);
     tot += M.norm[c] * __expf(-rho * M.inv2c[c]) * (ir * ir * ir);
   }
   return tot;
 }
 
-__device__ __forceinline__ void zv_point(const MixDev& M, int c, const double (&n)[3], double (&u)[3]) {
-  const double r = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-  const double cc = M.c[c];
-#pragma unroll
-  for (int l = 0; l < 3; l++) u[l] = cc * n[l] * r + M.G[3 * c + l];
-}
-
-// samples of one block: u1, u2 [3S] (double), w [S]
+// Samples of one block: u1, u2 [3S] (double), w [S].  Per sample one Philox4x32-10 call for
+// each electron: word 0 picks the mixture component (equal weights: floor(word * m / 2^32)),
+// words 1..3 give r ~ N(0, I3); the ZV map u = G_c + c |r| r (offset in FP32).
 __global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, MixDev M, double* __restrict__ u1,
                                      double* __restrict__ u2, double* __restrict__ w) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= S) return;
   const int64_t g = first + s;
-  double uu[8];
+  int d[2];
+  float off[2][3];
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    uint32_t cnt[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), (uint32_t)j, STREAM_SHARED};
+  for (int e = 0; e < 2; e++) {
+    uint32_t cnt[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), (uint32_t)e, STREAM_SHARED};
     philox4x32_10(cnt, (uint32_t)seed, (uint32_t)(seed >> 32));
-    uu[2 * j] = u01_open(cnt[0], cnt[1]);
-    uu[2 * j + 1] = u01_open(cnt[2], cnt[3]);
+    d[e] = (int)(((uint64_t)cnt[0] * (uint32_t)M.m) >> 32);
+    const float n0 = normal_from_word(cnt[1]), n1 = normal_from_word(cnt[2]), n2 = normal_from_word(cnt[3]);
+    const float sc = M.cf[d[e]] * sqrtf(fmaf(n0, n0, fmaf(n1, n1, n2 * n2)));
+    off[e][0] = sc * n0;
+    off[e][1] = sc * n1;
+    off[e][2] = sc * n2;
   }
-  const int c1 = pick_component(M, uu[0]);
-  const int c2 = pick_component(M, uu[4]);
-  double n1[3] = {normcdfinv(uu[1]), normcdfinv(uu[2]), normcdfinv(uu[3])};
-  double n2[3] = {normcdfinv(uu[5]), normcdfinv(uu[6]), normcdfinv(uu[7])};
-  double a[3], b[3];
-  zv_point(M, c1, n1, a);
-  zv_point(M, c2, n2, b);
-  const float p1 = mixture_density(M, a), p2 = mixture_density(M, b);
-  const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
-  const float r12 = (float)sqrt(dx * dx + dy * dy + dz * dz);
-  const float ww = 1.0f / (r12 * p1 * p2);
-  u1[3 * s] = a[0]; u1[3 * s + 1] = a[1]; u1[3 * s + 2] = a[2];
-  u2[3 * s] = b[0]; u2[3 * s + 1] = b[1]; u2[3 * s + 2] = b[2];
+  const float p1 = mixture_density(M, d[0], off[0]), p2 = mixture_density(M, d[1], off[1]);
+  float r2 = 0.f;
+#pragma unroll
+  for (int l = 0; l < 3; l++) {
+    const float dl = (M.Gf[3 * d[0] + l] - M.Gf[3 * d[1] + l]) +
+                     ((M.Glo[3 * d[0] + l] - M.Glo[3 * d[1] + l]) + (off[0][l] - off[1][l]));
+    r2 = fmaf(dl, dl, r2);
+    u1[3 * s + l] = M.G[3 * d[0] + l] + (double)off[0][l];
+    u2[3 * s + l] = M.G[3 * d[1] + l] + (double)off[1][l];
+  }
+  const float ww = 1.0f / (sqrtf(r2) * p1 * p2);
   w[s] = isfinite(ww) ? (double)ww : 0.0;
 }
 
@@ -383,25 +386,27 @@ static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
     }
   }
   const int m = (int)cc.size();
-  std::vector<double> cdf(m);
-  std::vector<float> Gf(3 * m), inv2c(m), norm(m);
+  std::vector<float> Gf(3 * m), Glo(3 * m), cf(m), inv2c(m), norm(m);
   const double wgt = 1.0 / m;
   const double k0 = pow(2.0 * M_PI, 1.5) * 2.0;
   for (int t = 0; t < m; t++) {
-    cdf[t] = (t == m - 1) ? 1.0 : (t + 1) * wgt;
-    for (int l = 0; l < 3; l++) Gf[3 * t + l] = (float)G[3 * t + l];
+    for (int l = 0; l < 3; l++) {
+      Gf[3 * t + l] = (float)G[3 * t + l];
+      Glo[3 * t + l] = (float)(G[3 * t + l] - (double)Gf[3 * t + l]);
+    }
+    cf[t] = (float)cc[t];
     inv2c[t] = (float)(1.0 / (2.0 * cc[t]));
     norm[t] = (float)(wgt / (k0 * pow(cc[t], 1.5)));
   }
-  double *dG, *dc, *dcdf;
-  float *dGf, *di2c, *dn;
+  double* dG;
+  float *dGf, *dGlo, *dcf, *di2c, *dn;
   TRY(upload_v(c, "sh_G", G, &dG));
-  TRY(upload_v(c, "sh_c", cc, &dc));
-  TRY(upload_v(c, "sh_cdf", cdf, &dcdf));
   TRY(upload_v(c, "sh_Gf", Gf, &dGf));
+  TRY(upload_v(c, "sh_Glo", Glo, &dGlo));
+  TRY(upload_v(c, "sh_cf", cf, &dcf));
   TRY(upload_v(c, "sh_i2c", inv2c, &di2c));
   TRY(upload_v(c, "sh_norm", norm, &dn));
-  S.mix = MixDev{m, dG, dc, dcdf, dGf, di2c, dn};
+  S.mix = MixDev{m, dG, dGf, dGlo, dcf, di2c, dn};
   TRY(upload_v(c, "sh_pi", S.pi, &S.d_pi));
   TRY(upload_v(c, "sh_pk", S.pk, &S.d_pk));
   TRY(upload_v(c, "sh_p1", S.p1, &S.d_p1));

@@ -159,9 +159,10 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     }
     count[bk] = (int64_t)work.size() - begin[bk];
   }
-  int rc = h2d(c, c->d_scratch_a, work.data(), sizeof(int64_t) * std::max<size_t>(work.size(), 1));
+  int rc = dev_alloc(c, c->d_scratch_b, sizeof(double) * std::max<int64_t>(nsel * split, 1));
   if (rc) return rc;
-  rc = dev_alloc(c, c->d_scratch_b, sizeof(double) * std::max<int64_t>(nsel * split, 1));
+  if (work.empty()) return SS_OK;  // e.g. a one-function basis: its only quartet is diagonal
+  rc = h2d(c, c->d_scratch_a, work.data(), sizeof(int64_t) * work.size());
   if (rc) return rc;
   const int64_t* d_work = (const int64_t*)c->d_scratch_a.ptr;
   double* d_partial = (double*)c->d_scratch_b.ptr;

@@ -80,3 +80,38 @@ def test_shared_split_bf16_vs_fp64(cfg, ng0, npts, nblocks):
     if ng0 == 20:  # the absolute gate is stated for the production 20-Gaussian fits, whose
         assert d.max() <= 1e-8, d.max()  # corrections are ~1e-7 Ha (4-Gaussian ones are ~1e-2 Ha)
     np.testing.assert_allclose(sigma, err, rtol=0.05, atol=1e-12)
+
+
+@pytest.mark.parametrize("zeta", [1.0, 1.7])
+def test_shared_estimator_sto_1s_known_answer(zeta):
+    """Analytic fit ERI + shared-walker correction = the exact unnormalised 1s STO
+    self-repulsion 5 pi^2 / (8 zeta^5) within 4 sigma (3-Gaussian fit: the fit alone is off by
+    many sigma), so the sampler's mixture density and weights carry no bias."""
+    import math
+    mol = basis.molecule_bohr(["H"], [[0.0, 0.0, 0.0]])
+    b = basis.build_basis(mol, {1: [("1S", zeta)]}, basis.FitParams(ng0=3))
+    q = basis.build_mapping(1)
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*q)
+        eri, sig = ctx.two_e_job(1.8, 7, 1 << 17, 10, "shared", "split_bf16")
+        g, _ = ctx.gauss_eri()
+    exact = 5 * math.pi ** 2 / (8 * zeta ** 5)
+    assert abs(g[0] - exact) > 10 * sig[0]
+    assert abs(eri[0] - exact) <= 4 * sig[0], (eri[0], exact, sig[0])
+
+
+def test_shared_agrees_with_faithful():
+    """Both estimators are unbiased for the same correction: on the 7-function H2O basis with
+    4-Gaussian fits (corrections ~1e-2 Ha) they agree within 5 combined sigma for all 406 ERIs."""
+    b, q = _setup("h2o_minimal", 4)
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*q)
+        ms, ss = ctx.zvmc(a_zv=1.8, seed=21, npts=1 << 16, nblocks=16, estimator="shared",
+                          precision="split_bf16")
+        mf, sf = ctx.zvmc(a_zv=1.8, seed=22, npts=40 * 400, nblocks=16, estimator="faithful",
+                          precision="fp64")
+    z = np.abs(ms - mf) / np.sqrt(ss ** 2 + sf ** 2 + 1e-300)
+    assert np.all(z <= 5.0), f"max |z| {z.max():.2f}"
+    assert np.mean(z) < 1.2  # |N(0,1)| averages 0.80
