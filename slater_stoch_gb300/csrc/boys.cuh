@@ -154,6 +154,46 @@ SS_HD void boys_tab(double T, int nf, double (&F)[NF + 1], const double* tab) {
   }
 }
 
+// Single-precision Boys values F_0..F_nf(T) for the primitive quartets evaluated in FP32
+// (relative error ~1e-7 plus the conditioning of T itself).  T < 30: F_nf from the Taylor series
+// around T_k = k/8 with 6 terms (table rows F_n(T_k), n = 0..21, rounded to float), then the
+// stable downward recursion F_n = (2T F_{n+1} + e^-T)/(2n+1).  T >= 30: F_0 = sqrt(pi/T)/2
+// (erf(sqrt T) = 1 to 1e-14) and the upward recursion F_n = ((2n-1) F_{n-1} - e^-T)/(2T), stable
+// there since (2n-1)/(2T) < 1.  tab32 = BOYS32_K x BOYS32_N floats.
+template <int NF>
+SS_HD void boys32(float T, int nf, float (&F)[NF + 1], const float* tab32) {
+  static_assert(NF + 6 <= BOYS32_N, "FP32 Boys table too short for this order");
+  if (T >= 30.f) {
+    const float h = 0.5f / T;
+    const float e = expf(-T);
+    float f = 0.886226925452758f * sqrtf(h + h);  // sqrt(pi)/2 / sqrt(T)
+    F[0] = f;
+#pragma unroll
+    for (int n = 1; n <= NF; n++) {
+      if (n > nf) break;
+      f = fmaf((float)(2 * n - 1), f, -e) * h;
+      F[n] = f;
+    }
+    return;
+  }
+  const int k = (int)(T * 8.f + 0.5f);
+  const float x = (float)k * 0.125f - T;  // T_k - T
+  const float* f = tab32 + k * BOYS32_N + nf;
+  float s = f[5];
+  s = fmaf(s, x * 0.2f, f[4]);
+  s = fmaf(s, x * 0.25f, f[3]);
+  s = fmaf(s, x * (1.f / 3.f), f[2]);
+  s = fmaf(s, x * 0.5f, f[1]);
+  s = fmaf(s, x, f[0]);
+  const float e = expf(-T);
+  F[NF] = 0.f;
+#pragma unroll
+  for (int n = NF; n >= 0; n--) {
+    if (n == nf) F[n] = s;
+    else if (n < nf) F[n] = fmaf(T + T, F[n + 1 <= NF ? n + 1 : NF], e) * (1.f / (float)(2 * n + 1));
+  }
+}
+
 #ifdef __CUDACC__
 // cooperative copy of the three tables into shared memory (call before the first use, followed
 // by a __syncthreads)

@@ -111,7 +111,7 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
 // partial sums -> ERIs; diagonal reuse and Schwarz screening (src/two_e_slater.F90:264-279)
 __global__ void eri_finalize(int64_t nint, const int32_t* __restrict__ is, const int32_t* __restrict__ js,
                              const int32_t* __restrict__ ks, const int32_t* __restrict__ ls,
-                             const int64_t* __restrict__ slot, int split, const double* __restrict__ partial,
+                             const int64_t* __restrict__ slot, const double* __restrict__ partial,
                              const double* __restrict__ pre, int n, double* __restrict__ out) {
   int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= nint) return;
@@ -124,24 +124,11 @@ __global__ void eri_finalize(int64_t nint, const int32_t* __restrict__ is, const
     v = 0.0;
   } else {
     v = 0.0;
-    for (int t = 0; t < split; t++) v = v + partial[s * split + t];
+    const int64_t o = slot_offset(s);
+    const int sp = slot_split(s);
+    for (int t = 0; t < sp; t++) v = v + partial[o + t];
   }
   out[q] = v;
-}
-
-__global__ void precond_finalize(int n, int split, const double* __restrict__ partial,
-                                 double* __restrict__ pre) {
-  int64_t pidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t np = (int64_t)n * (n + 1) / 2;
-  if (pidx >= np) return;
-  int i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
-  while ((int64_t)i * (i + 1) / 2 > pidx) i--;
-  while ((int64_t)(i + 1) * (i + 2) / 2 <= pidx) i++;
-  int k = (int)(pidx - (int64_t)i * (i + 1) / 2);
-  double v = 0.0;
-  for (int t = 0; t < split; t++) v = v + partial[pidx * split + t];
-  pre[i + (int64_t)n * k] = v;
-  pre[k + (int64_t)n * i] = v;
 }
 
 // Launch helpers ------------------------------------------------------------------------
@@ -150,12 +137,14 @@ cudaError_t eri_init_constants() { return cudaSuccess; }  // tables are compile-
 // ket pairs per shared-memory tile and the dynamic shared memory it needs
 void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
   const int no = t2 ? 4 : 1;
-  const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (L + 1);
+  // per ket pair: the record and its polynomials in FP64, and their FP32 copies
+  const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (L + 1) + 6 * sizeof(float) +
+                     sizeof(float) * 3 * no * (L + 1);
   // Classes with r^2-type fits keep their per-item recursion tables and option polynomials in
   // local memory: a small ket tile leaves the SM's unified L1 to them (measured on the 26-function
   // H2O basis: 200 KB -> 40 KB tiles took these classes from 3.6 s to 2.7 s).  The other classes
   // keep their working set in registers and take the largest tile.
-  const size_t budget = (t2 ? 40u : 200u) * 1024u;
+  const size_t budget = (t2 ? 40u : 168u) * 1024u;  // + ~53 KB of static tables and scans
   int kt = (int)(budget / per);
   kt = kt < max_cnt ? kt : max_cnt;
   kt = kt < 1 ? 1 : kt;
@@ -163,43 +152,46 @@ void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
   *smem = per * kt;
 }
 
-cudaError_t launch_eri_L0c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L1c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L2c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L3c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L2c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L3c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L2c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
-cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*);
+cudaError_t launch_eri_L0c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L1c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c4(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 
 // Kernel instance for class (L, tc).  tc: number of r^2-type fits among the four functions
-// (0, 1, 2, 3 = three or four).  A quartet with r^2-type fits has L >= 2, and one with three or
-// four has L = 4; an instance with a larger L serves any smaller one (degrees are runtime).
+// (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has L = 4; an
+// instance with a larger L serves any smaller one (degrees are runtime).
 cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
-                             double* partial, double* self_out) {
+                             double* partial, double* self_out, const PrimPairF* ppf) {
   if (tc == 0) {
-    if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 2) return launch_eri_L2c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 3) return launch_eri_L3c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 4) return launch_eri_L4c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 2) return launch_eri_L2c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
   } else if (tc == 1) {
-    if (L <= 2) return launch_eri_L2c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 3) return launch_eri_L3c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 4) return launch_eri_L4c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L <= 2) return launch_eri_L2c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
   } else if (tc == 2) {
-    if (L <= 2) return launch_eri_L2c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 3) return launch_eri_L3c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
-    if (L == 4) return launch_eri_L4c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L <= 2) return launch_eri_L2c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
   } else if (tc == 3) {
-    if (L <= 4) return launch_eri_L4c3(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out);
+    if (L <= 4) return launch_eri_L4c3(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+  } else if (tc == 4) {
+    if (L <= 4) return launch_eri_L4c4(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
   }
   return cudaErrorInvalidValue;
 }
@@ -240,6 +232,25 @@ __global__ void __launch_bounds__(512) prim_pair_sort(const PrimPair* __restrict
       __syncthreads();
     }
   for (int t = threadIdx.x; t < m; t += blockDim.x) dst[t] = src[s_idx[t]];
+}
+
+// FP32 copies of the (sorted) primitive pairs, fc = K_AB * coefficient product
+__global__ void prim_pair_to_f32(int64_t npp, const PrimPair* __restrict__ in, PrimPairF* __restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= npp) return;
+  const PrimPair a = in[t];
+  PrimPairF f;
+  f.p = (float)a.p;
+  f.p_inv = (float)a.p_inv;
+  f.fc = (float)(a.fact * a.coef);
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++) {
+    f.P[ax] = (float)a.P[ax];
+    f.PA[ax] = (float)a.PA[ax];
+    f.PB[ax] = (float)a.PB[ax];
+  }
+  f.pad[0] = f.pad[1] = 0.f;
+  out[t] = f;
 }
 
 }  // namespace ss

@@ -35,41 +35,41 @@ constexpr double PI_5_2 = 34.9868366552;  // src/general_primitive_integral.F90:
 // (x - x_A)^a around x_P: coefficients of (x-x_P)^i, pw1 = x_P - x_A
 // (src/give_explicit_poly_and_gaussian.F90:86-220, cases 0..4; the powers and the exact
 // integer binomials of each case)
-template <int L>
-__device__ __forceinline__ void recentered(double pw1, int a, double (&P)[L + 1]) {
+template <int L, typename Real>
+__device__ __forceinline__ void recentered(Real pw1, int a, Real (&P)[L + 1]) {
 #pragma unroll
-  for (int t = 0; t <= L; t++) P[t] = 0.0;
+  for (int t = 0; t <= L; t++) P[t] = Real(0);
   if (a == 0) {
-    P[0] = 1.0;
+    P[0] = Real(1);
   } else if (a == 1) {
     P[0] = pw1;
-    if (L >= 1) P[1 % (L + 1)] = 1.0;
+    if (L >= 1) P[1 % (L + 1)] = Real(1);
   } else if (a == 2) {
-    const double p2 = pw1 * pw1;
+    const Real p2 = pw1 * pw1;
     P[0] = p2;
-    if (L >= 2) { P[1 % (L + 1)] = 2.0 * pw1; P[2 % (L + 1)] = 1.0; }
+    if (L >= 2) { P[1 % (L + 1)] = Real(2) * pw1; P[2 % (L + 1)] = Real(1); }
   } else if (a == 3) {
-    const double p2 = pw1 * pw1, p3 = p2 * pw1;
+    const Real p2 = pw1 * pw1, p3 = p2 * pw1;
     P[0] = p3;
-    if (L >= 3) { P[1 % (L + 1)] = 3.0 * p2; P[2 % (L + 1)] = 3.0 * pw1; P[3 % (L + 1)] = 1.0; }
+    if (L >= 3) { P[1 % (L + 1)] = Real(3) * p2; P[2 % (L + 1)] = Real(3) * pw1; P[3 % (L + 1)] = Real(1); }
   } else {  // a == 4
-    const double p2 = pw1 * pw1, p3 = p2 * pw1, p4 = p2 * p2;
+    const Real p2 = pw1 * pw1, p3 = p2 * pw1, p4 = p2 * p2;
     P[0] = p4;
     if (L >= 4) {
-      P[1 % (L + 1)] = 4.0 * p3; P[2 % (L + 1)] = 6.0 * p2; P[3 % (L + 1)] = 4.0 * pw1;
-      P[4 % (L + 1)] = 1.0;
+      P[1 % (L + 1)] = Real(4) * p3; P[2 % (L + 1)] = Real(6) * p2; P[3 % (L + 1)] = Real(4) * pw1;
+      P[4 % (L + 1)] = Real(1);
     }
   }
 }
 
 // P_new = recentered(A,a) * recentered(B,b) in multiply_poly's order (src/multiply_poly.F90:22-31)
-template <int L>
-__device__ __forceinline__ void pair_poly(double pa, int a, double pb, int b, double* Pn) {
-  double Pa[L + 1], Pb[L + 1];
-  recentered<L>(pa, a, Pa);
-  recentered<L>(pb, b, Pb);
+template <int L, typename Real>
+__device__ __forceinline__ void pair_poly(Real pa, int a, Real pb, int b, Real* Pn) {
+  Real Pa[L + 1], Pb[L + 1];
+  recentered<L, Real>(pa, a, Pa);
+  recentered<L, Real>(pb, b, Pb);
 #pragma unroll
-  for (int t = 0; t <= L; t++) Pn[t] = 0.0;
+  for (int t = 0; t <= L; t++) Pn[t] = Real(0);
 #pragma unroll
   for (int ib = 0; ib <= L; ib++)
 #pragma unroll
@@ -77,29 +77,30 @@ __device__ __forceinline__ void pair_poly(double pa, int a, double pb, int b, do
       if (ib + ic <= L && ib <= a && ic <= b) Pn[ib + ic] = Pn[ib + ic] + Pb[ic] * Pa[ib];
 }
 
-struct RecCoef {
-  double p10_1, p10_2, p01_1, p01_2, pq_inv;
+template <typename Real>
+struct RecCoefT {
+  Real p10_1, p10_2, p01_1, p01_2, pq_inv;
 };
 
 // Bottom-up table I(a,c)[m] (coefficients of u = t^2) for a <= amax, c <= cmax (both <= L),
 // the same per-coefficient operation order as I_x1_pol_mult / I_x2_pol_mult:
 //   I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1);  I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
-template <int L>
-__device__ __forceinline__ void rys_table(const RecCoef& R, double Cc, double Dd, int amax, int cmax,
-                                          double (&I)[L + 1][L + 1][2 * L + 1]) {
+template <int L, typename Real>
+__device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int cmax,
+                                          Real (&I)[L + 1][L + 1][2 * L + 1]) {
 #pragma unroll
   for (int c = 0; c <= L; c++) {
     if (c > cmax) break;
 #pragma unroll
     for (int m = 0; m <= 2 * L; m++) {
       if (m > c) break;
-      double v = 0.0;
+      Real v = Real(0);
       if (c == 0) {
-        v = 1.0;
+        v = Real(1);
       } else {
         if (c >= 2) {
-          if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (double)(c - 1));
-          if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (double)(c - 1));
+          if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (Real)(c - 1));
+          if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (Real)(c - 1));
         }
         if (m >= 1) v = v + Dd * I[0][c - 1][m - 1];
       }
@@ -115,13 +116,13 @@ __device__ __forceinline__ void rys_table(const RecCoef& R, double Cc, double Dd
 #pragma unroll
       for (int m = 0; m <= 2 * L; m++) {
         if (m > a + c) break;
-        double v = 0.0;
+        Real v = Real(0);
         if (a >= 2) {
-          const double s = (double)(a - 1);
+          const Real s = (Real)(a - 1);
           if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
           if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
         }
-        if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (double)c);
+        if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (Real)c);
         if (m >= 1) v = v + Cc * I[a - 1][c][m - 1];
         I[a][c][m] = v;
       }
@@ -131,21 +132,21 @@ __device__ __forceinline__ void rys_table(const RecCoef& R, double Cc, double Dd
 
 // The same table when bra and ket share one centre (all four functions on one atom): C00 and
 // D00 vanish, so only the B10/B01/B00 terms remain and every entry with a + c odd is zero.
-template <int L>
-__device__ __forceinline__ void rys_table_1c(const RecCoef& R, int amax, int cmax,
-                                             double (&I)[L + 1][L + 1][2 * L + 1]) {
+template <int L, typename Real>
+__device__ __forceinline__ void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
+                                             Real (&I)[L + 1][L + 1][2 * L + 1]) {
 #pragma unroll
   for (int c = 0; c <= L; c++) {
     if (c > cmax) break;
 #pragma unroll
     for (int m = 0; m <= 2 * L; m++) {
       if (m > c) break;
-      double v = 0.0;
+      Real v = Real(0);
       if (c == 0) {
-        v = 1.0;
+        v = Real(1);
       } else if (!(c & 1) && c >= 2) {
-        if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (double)(c - 1));
-        if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (double)(c - 1));
+        if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (Real)(c - 1));
+        if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (Real)(c - 1));
       }
       I[0][c][m] = v;
     }
@@ -159,14 +160,14 @@ __device__ __forceinline__ void rys_table_1c(const RecCoef& R, int amax, int cma
 #pragma unroll
       for (int m = 0; m <= 2 * L; m++) {
         if (m > a + c) break;
-        double v = 0.0;
+        Real v = Real(0);
         if (!((a + c) & 1)) {
           if (a >= 2) {
-            const double s = (double)(a - 1);
+            const Real s = (Real)(a - 1);
             if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
             if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
           }
-          if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (double)c);
+          if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (Real)c);
         }
         I[a][c][m] = v;
       }
@@ -181,25 +182,27 @@ __device__ __forceinline__ bool abs_lt(double x, double t) {
 __device__ __forceinline__ bool abs_gt(double x, double t) {
   return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(t);
 }
+__device__ __forceinline__ bool abs_lt(float x, float t) { return (__float_as_int(x) & 0x7FFFFFFF) < __float_as_int(t); }
+__device__ __forceinline__ bool abs_gt(float x, float t) { return (__float_as_int(x) & 0x7FFFFFFF) > __float_as_int(t); }
 
 // Ix = sum_{ix,jx} (Pn[ix] Qn[jx]) I(ix,jx) with the thresholds of general_primitive_integral
 // (x axis: skip |P| < thresh; y, z: keep |P| > thresh; skip |P Q| < thresh).
-template <int L>
-__device__ __forceinline__ void axis_poly(const double* Pn, int degP, const double* Qn, int degQ,
-                                          const double (&I)[L + 1][L + 1][2 * L + 1], bool x_axis,
-                                          double* out) {
+template <int L, typename Real>
+__device__ __forceinline__ void axis_poly(const Real* Pn, int degP, const Real* Qn, int degQ,
+                                          const Real (&I)[L + 1][L + 1][2 * L + 1], bool x_axis,
+                                          Real* out) {
 #pragma unroll
-  for (int m = 0; m <= 2 * L; m++) out[m] = 0.0;
+  for (int m = 0; m <= 2 * L; m++) out[m] = Real(0);
 #pragma unroll
   for (int ix = 0; ix <= L; ix++) {
     if (ix > degP) break;
-    const double a = Pn[ix];
-    if (x_axis ? abs_lt(a, THRESH) : !abs_gt(a, THRESH)) continue;
+    const Real a = Pn[ix];
+    if (x_axis ? abs_lt(a, (Real)THRESH) : !abs_gt(a, (Real)THRESH)) continue;
 #pragma unroll
     for (int jx = 0; jx <= L; jx++) {
       if (jx > degQ) break;
-      const double d = a * Qn[jx];
-      if (abs_lt(d, THRESH)) continue;
+      const Real d = a * Qn[jx];
+      if (abs_lt(d, (Real)THRESH)) continue;
 #pragma unroll
       for (int m = 0; m <= 2 * L; m++)
         if (m <= ix + jx) out[m] = fma(d, I[ix][jx][m], out[m]);
@@ -267,8 +270,8 @@ __device__ __forceinline__ void subset_options(const QuartetShape& S, int s, int
 
 // recentred pair polynomials of a primitive pair, per (axis, option); side 0 = bra (functions
 // i, k), side 1 = ket (functions j, l).  Layout [ax][o][L+1].
-template <int L, bool T2>
-__device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, const PrimPair& P, double* out) {
+template <int L, bool T2, typename Real, typename Rec>
+__device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, const Rec& P, Real* out) {
   constexpr int NO = T2 ? 4 : 1;
   const int f0 = 2 * side, f1 = 2 * side + 1;
 #pragma unroll
@@ -277,65 +280,85 @@ __device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, cons
     for (int o = 0; o < NO; o++) {
       if ((o & 1) && !S.t2[f0]) continue;
       if ((o & 2) && !S.t2[f1]) continue;
-      pair_poly<L>(P.PA[ax], S.np[f0][ax] + 2 * (o & 1), P.PB[ax], S.np[f1][ax] + (o & 2),
-                   out + (ax * NO + o) * (L + 1));
+      pair_poly<L, Real>(P.PA[ax], S.np[f0][ax] + 2 * (o & 1), P.PB[ax], S.np[f1][ax] + (o & 2),
+                         out + (ax * NO + o) * (L + 1));
     }
+}
+
+// The fields of a primitive pair that one primitive quartet reads, in the arithmetic type of the
+// evaluation (FP64, or FP32 for the quartets below the FP32 bound).
+template <typename Real>
+struct PairView {
+  Real p, p_inv, P[3], fact;
+};
+
+__device__ __forceinline__ PairView<double> view64(const PrimPair& A) {
+  return PairView<double>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fact};
+}
+
+// FP32 view: fact carries K_AB times the coefficient product, so the FP32 quartet value comes
+// out already multiplied by the coefficients
+__device__ __forceinline__ PairView<float> view32(const PrimPairF& A) {
+  return PairView<float>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fc};
 }
 
 // One primitive quartet (src/general_primitive_integral.F90, summed over the cartesian
 // components of the r^2-type fits): returns pref * sum_n d1[n] F_n; the caller multiplies by
 // the coefficient product P.coef * Q.coef.  Pn, Qn: pair_polys of the bra and ket pairs.
-// TC: 0 = no r^2-type fit; 1, 2 = exactly one / two of them (subset recursion over the axes,
-// below); 3 = three or four (all cartesian combinations enumerated).
-template <int L, int TC>
-__device__ __forceinline__ double prim_quartet(const QuartetShape& S, const PrimPair& P, const double* Pn,
-                                               const PrimPair& Q, const double* Qn, const double* s_boys) {
+// TC: the number of r^2-type fits among the four functions (0..4; with any, the subset recursion
+// over the axes below).
+template <int L, int TC, typename Real>
+__device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const Real* Pn,
+                                             const PairView<Real>& Q, const Real* Qn, const Real* s_boys) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;
   constexpr int NF = (6 * L < 16) ? 6 * L : 16;
-  const double p = P.p, qq = Q.p;
+  const Real p = P.p, qq = Q.p;
   // src/general_primitive_integral.F90:54-60, 142-146
-  const double pq = P.p_inv * 0.5 * Q.p_inv;
-  const double rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
-  const double pq_inv = 0.5 * (rs_pq * rs_pq);
-  RecCoef R;
+  const Real pq = P.p_inv * Real(0.5) * Q.p_inv;
+  const Real rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
+  const Real pq_inv = Real(0.5) * (rs_pq * rs_pq);
+  RecCoefT<Real> R;
   R.p10_1 = qq * pq;
   R.p01_1 = p * pq;
-  const double pq_inv_2 = pq_inv + pq_inv;
+  const Real pq_inv_2 = pq_inv + pq_inv;
   R.p10_2 = pq_inv_2 * R.p10_1 * qq;
   R.p01_2 = pq_inv_2 * R.p01_1 * p;
   R.pq_inv = pq_inv;
-  const double rho = p * qq * pq_inv_2;
-  const double dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
-  const double T = (dx * dx + dy * dy + dz * dz) * rho;
-  double F[NF + 1];
-  boys_tab<NF>(T, S.nf, F, s_boys);
+  const Real rho = p * qq * pq_inv_2;
+  const Real dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
+  const Real T = (dx * dx + dy * dy + dz * dz) * rho;
+  Real F[NF + 1];
+  if constexpr (sizeof(Real) == 8)
+    boys_tab<NF>(T, S.nf, F, s_boys);
+  else
+    boys32<NF>(T, S.nf, F, s_boys);
   const int nf = S.nf;
 
-  double accu;
+  Real accu;
   if (!T2) {
-    double A[3][2 * L + 1];
+    Real A[3][2 * L + 1];
     int deg[3];
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       deg[ax] = S.amax[ax] + S.cmax[ax];
       if (deg[ax] == 0) {
-        A[ax][0] = 1.0;
+        A[ax][0] = Real(1);
 #pragma unroll
-        for (int m = 1; m <= 2 * L; m++) A[ax][m] = 0.0;
+        for (int m = 1; m <= 2 * L; m++) A[ax][m] = Real(0);
         continue;
       }
-      double I[L + 1][L + 1][2 * L + 1];
-      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
-      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
+      Real I[L + 1][L + 1][2 * L + 1];
+      const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
+      const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
       if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
       else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       axis_poly<L>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (L + 1), S.cmax[ax], I, ax == 0, A[ax]);
     }
     // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
-    double dp[4 * L + 1];
+    Real dp[4 * L + 1];
 #pragma unroll
-    for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
+    for (int t = 0; t <= 4 * L; t++) dp[t] = Real(0);
 #pragma unroll
     for (int a = 0; a <= 2 * L; a++) {
       if (a > deg[0]) break;
@@ -345,9 +368,9 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
         dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
       }
     }
-    double d1[NF + 1];
+    Real d1[NF + 1];
 #pragma unroll
-    for (int t = 0; t <= NF; t++) d1[t] = 0.0;
+    for (int t = 0; t <= NF; t++) d1[t] = Real(0);
 #pragma unroll
     for (int a = 0; a <= 4 * L; a++) {
       if (a > deg[0] + deg[1] || a > NF) break;
@@ -361,20 +384,21 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
 #pragma unroll
     for (int n = 1; n <= NF; n++)
       if (n <= nf) accu = fma(d1[n], F[n], accu);
-  } else if (TC == 1 || TC == 2) {
+  } else {
     // With t = TC r^2-type fits, a cartesian combination assigns each fit's +2 to one axis, i.e.
     // splits the set of fits into (Sx, Sy, Sz).  sum over combinations of L(Ax[Sx] Ay[Sy] Az[Sz])
     // is built axis by axis: Qxy[S] = sum_{Sx subset S} Ax[Sx] Ay[S \ Sx], then
     // sum_Sz L(Qxy[all \ Sz] Az[Sz]), L(p) = sum_n p[n] F_n.  Same per-axis polynomials (and
     // thresholds) as the enumeration of the 3^t combinations, 2^t final contractions instead of 3^t.
-    constexpr int NS = 1 << (TC == 1 ? 1 : 2);
-    double Ax[NS][2 * L + 1], Qxy[NS][4 * L + 1];
+    constexpr int NS = 1 << TC;
+    constexpr int full = NS - 1;
+    Real Ax[NS][2 * L + 1], Qxy[NS][4 * L + 1];
     int dAx[NS], dQ[NS];
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
-      double I[L + 1][L + 1][2 * L + 1];
-      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
-      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
+      Real I[L + 1][L + 1][2 * L + 1];
+      const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
+      const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
       if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
       else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       if (ax == 1) {
@@ -382,7 +406,7 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
         for (int t = 0; t < NS; t++) {
           dQ[t] = -1;
 #pragma unroll
-          for (int m = 0; m <= 4 * L; m++) Qxy[t][m] = 0.0;
+          for (int m = 0; m <= 4 * L; m++) Qxy[t][m] = Real(0);
         }
       }
 #pragma unroll
@@ -391,7 +415,7 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
         subset_options(S, sa, ob, oc);
         const int da = S.np[0][ax] + S.np[1][ax] + 2 * (ob & 1) + (ob & 2);
         const int dc = S.np[2][ax] + S.np[3][ax] + 2 * (oc & 1) + (oc & 2);
-        double Aa[2 * L + 1];
+        Real Aa[2 * L + 1];
         axis_poly<L>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0, Aa);
         const int dA = da + dc;
         if (ax == 0) {
@@ -415,12 +439,12 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
             }
           }
         } else {
-          const int st = (NS - 1) ^ sa;
-          double sum = 0.0;
+          const int st = full ^ sa;
+          Real sum = Real(0);
 #pragma unroll
           for (int c = 0; c <= 2 * L; c++) {
             if (c > dA) break;
-            double g = 0.0;
+            Real g = Real(0);
 #pragma unroll
             for (int a = 0; a <= 4 * L; a++) {
               if (a > dQ[st] || a + c > NF) break;
@@ -432,82 +456,9 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
         }
       }
     }
-  } else {
-    // axis polynomials for every (bra option, ket option), then the cartesian combinations
-    double A[3][NO * NO][2 * L + 1];
-#pragma unroll 1
-    for (int ax = 0; ax < 3; ax++) {
-      double I[L + 1][L + 1][2 * L + 1];
-      const double Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
-      const double Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
-      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
-      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
-#pragma unroll 1
-      for (int ob = 0; ob < NO; ob++) {
-        if ((ob & 1) && !S.t2[0]) continue;
-        if ((ob & 2) && !S.t2[1]) continue;
-#pragma unroll 1
-        for (int oc = 0; oc < NO; oc++) {
-          if ((oc & 1) && !S.t2[2]) continue;
-          if ((oc & 2) && !S.t2[3]) continue;
-          const int da = S.np[0][ax] + S.np[1][ax] + 2 * (ob & 1) + (ob & 2);
-          const int dc = S.np[2][ax] + S.np[3][ax] + 2 * (oc & 1) + (oc & 2);
-          axis_poly<L>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0,
-                       A[ax][ob * NO + oc]);
-        }
-      }
-    }
-    accu = 0.0;
-    const int nci = S.t2[0] ? 3 : 1, nck = S.t2[1] ? 3 : 1, ncj = S.t2[2] ? 3 : 1, ncl = S.t2[3] ? 3 : 1;
-    for (int ci = 0; ci < nci; ci++)
-      for (int ck = 0; ck < nck; ck++)
-        for (int cj = 0; cj < ncj; cj++)
-          for (int cl = 0; cl < ncl; cl++) {
-            int sel[3], deg[3];
-#pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-              const int ob = (S.t2[0] && ci == ax ? 1 : 0) | (S.t2[1] && ck == ax ? 2 : 0);
-              const int oc = (S.t2[2] && cj == ax ? 1 : 0) | (S.t2[3] && cl == ax ? 2 : 0);
-              sel[ax] = ob * NO + oc;
-              deg[ax] = S.np[0][ax] + S.np[1][ax] + S.np[2][ax] + S.np[3][ax] +
-                        2 * ((ob & 1) + (ob >> 1) + (oc & 1) + (oc >> 1));
-            }
-            const double* Ax = A[0][sel[0]];
-            const double* Ay = A[1][sel[1]];
-            const double* Az = A[2][sel[2]];
-            double dp[4 * L + 1];
-#pragma unroll
-            for (int t = 0; t <= 4 * L; t++) dp[t] = 0.0;
-#pragma unroll
-            for (int a = 0; a <= 2 * L; a++) {
-              if (a > deg[0]) break;
-#pragma unroll
-              for (int c = 0; c <= 2 * L; c++) {
-                if (c > deg[1]) break;
-                dp[a + c] = fma(Ay[c], Ax[a], dp[a + c]);
-              }
-            }
-            double d1[NF + 1];
-#pragma unroll
-            for (int t = 0; t <= NF; t++) d1[t] = 0.0;
-#pragma unroll
-            for (int a = 0; a <= 4 * L; a++) {
-              if (a > deg[0] + deg[1] || a > NF) break;
-#pragma unroll
-              for (int c = 0; c <= 2 * L; c++) {
-                if (c > deg[2] || a + c > NF) break;
-                d1[a + c] = fma(Az[c], dp[a], d1[a + c]);
-              }
-            }
-            double sum = d1[0] * F[0];
-#pragma unroll
-            for (int n = 1; n <= NF; n++)
-              if (n <= nf) sum = fma(d1[n], F[n], sum);
-            accu = accu + sum;
-          }
   }
   // src/general_primitive_integral.F90:192
-  const double pref = P.fact * Q.fact * PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
+  const Real pref = P.fact * Q.fact * (Real)PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
   return pref * accu;
 }
 
@@ -518,10 +469,14 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
 // Primitive screening (pre != nullptr): the primitive pairs of every function pair are sorted
 // by decreasing Schwarz factor S; a primitive quartet with S_P S_Q < eps sqrt((ik|ik)(jl|jl))
 // is skipped.  Each skipped term is bounded by that product, so the skipped part of an ERI is at
-// most (number of primitive quartets) * eps * sqrt((ik|ik)(jl|jl)).  For each bra pair the kept
-// ket pairs of a tile are a prefix of the tile; the kept items of the tile are numbered through
-// an exclusive scan of the per-bra prefix lengths.  Without pre every item is kept (the Schwarz
-// diagonal itself).  The items are spread evenly over the threads (to within one).
+// most (number of primitive quartets) * eps * sqrt((ik|ik)(jl|jl)).
+// FP32 tier (pre != nullptr): a kept primitive quartet with S_P S_Q < eps32 sqrt((ik|ik)(jl|jl))
+// is evaluated in FP32 (PRIM_FP32_EPS in ss_common.cuh gives the error bound).
+// For each bra pair the FP64 and the FP32 ket pairs of a tile are consecutive ranges from the
+// start of the tile (the ket factors decrease along it); the items of each tier are numbered
+// through an exclusive scan of the per-bra range lengths.  Without pre every item is FP64 and
+// kept (the Schwarz diagonal itself).  The items of a tier are spread evenly over the threads
+// (to within one).
 //
 // Schwarz-factor mode (self_out != nullptr; work = the quartets (ik|ik)): only the items (P, P)
 // are evaluated and S_P = sqrt(c_P^2 (P|P)), the self-repulsion of the primitive pair's charge
@@ -529,24 +484,29 @@ __device__ __forceinline__ double prim_quartet(const QuartetShape& S, const Prim
 // is written to self_out[16 * (pair_off + P)] (PrimPair::pad[0] of the pair).  By
 // Cauchy-Schwarz |c_P c_Q (P|Q)| <= S_P S_Q for every primitive quartet.
 // TC: how many of the four functions are r^2-type fits (3 cartesian components sharing
-// exponents): 0, 1, 2, or 3 for three or four.
+// exponents), 0..4.
 template <int L, int TC>
 __global__ void __launch_bounds__(128) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
     const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
     const int32_t* __restrict__ ls, const double* __restrict__ pre, double eps, double* __restrict__ partial,
-    double* __restrict__ self_out) {
+    double* __restrict__ self_out, const PrimPairF* __restrict__ ppf) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
-  constexpr int QW = 3 * NO * (L + 1);  // ket polynomial doubles per ket pair
+  constexpr int QW = 3 * NO * (L + 1);  // ket polynomial values per ket pair
   extern __shared__ double2 s_raw[];
   PrimPair* s_ket = reinterpret_cast<PrimPair*>(s_raw);
   double* s_q = reinterpret_cast<double*>(s_ket + ktile);
+  PairView<float>* s_ketf = reinterpret_cast<PairView<float>*>(s_q + (size_t)ktile * QW);
+  float* s_qf = reinterpret_cast<float*>(s_ketf + ktile);
   __shared__ double s_red[4];
-  __shared__ int s_scan[SS_MAX_NG * SS_MAX_NG + 1];  // kept-item offsets of the bra slice
+  __shared__ int s_scan[SS_MAX_NG * SS_MAX_NG + 1];    // FP64 item offsets of the bra slice
+  __shared__ int s_scan32[SS_MAX_NG * SS_MAX_NG + 1];  // FP32 item offsets
   __shared__ double s_boys[BOYS_SMEM_DOUBLES];
+  __shared__ float s_boys32[BOYS32_K * BOYS32_N];
   boys_tables_to_smem(s_boys);  // ordered before first use by the tile loop's barriers
+  for (int t = threadIdx.x; t < BOYS32_K * BOYS32_N; t += blockDim.x) s_boys32[t] = boys32_tab[t];
 
   const int64_t w = blockIdx.x / split;
   const int part = blockIdx.x % split;
@@ -556,15 +516,21 @@ __global__ void __launch_bounds__(128) eri_kernel(
   const int nb = pair_cnt[pb], nk = pair_cnt[pk];
   const PrimPair* bra = pp + pair_off[pb];
   const PrimPair* ket = pp + pair_off[pk];
+  const PrimPairF* braf = ppf + pair_off[pb];
+  const PrimPairF* ketf = ppf + pair_off[pk];
   const QuartetShape S = quartet_shape<T2>(B, fi, fk, fj, fl);
   const int n = B.n;
-  const double tau = pre ? eps * sqrt(pre[fi + (int64_t)n * fk] * pre[fj + (int64_t)n * fl]) : 0.0;
+  const double sch = pre ? sqrt(pre[fi + (int64_t)n * fk] * pre[fj + (int64_t)n * fl]) : 0.0;
+  // the FP32 tier needs the Schwarz diagonal and the FP32 pair copies (not in self mode)
+  const bool fp32_tier = pre != nullptr && ppf != nullptr && self_out == nullptr;
+  const double tau = eps * sch, tau32 = fp32_tier ? PRIM_FP32_EPS * sch : 0.0;
 
   const int per = (nb + split - 1) / split;
   const int b0 = part * per;
   const int b1 = min(nb, b0 + per);
   const int nbs = max(b1 - b0, 0);
   double acc = 0.0;
+  float acc32 = 0.f;
 
   for (int t0 = 0; t0 < nk; t0 += ktile) {
     const int kt = min(ktile, nk - t0);
@@ -574,70 +540,114 @@ __global__ void __launch_bounds__(128) eri_kernel(
       for (int t = threadIdx.x; t < kt * 8; t += blockDim.x) s_raw[t] = src[t];
     }
     __syncthreads();
-    // recentred ket polynomials, per (ket pair, axis, option)
-    for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) pair_polys<L, T2>(S, 1, s_ket[kk], s_q + (size_t)kk * QW);
-    // kept ket prefix of every bra pair of the slice (ket factors decrease along the tile)
+    // recentred ket polynomials, per (ket pair, axis, option), and their FP32 copies
+    for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) {
+      double* qd = s_q + (size_t)kk * QW;
+      pair_polys<L, T2, double>(S, 1, s_ket[kk], qd);
+      if (fp32_tier) {
+        float* qf = s_qf + (size_t)kk * QW;
+#pragma unroll
+        for (int t = 0; t < QW; t++) qf[t] = (float)qd[t];
+        s_ketf[kk] = view32(ketf[t0 + kk]);
+      }
+    }
+    // per bra pair of the slice: the ket ranges [0, c64) in FP64 and [c64, c) in FP32
     for (int bi = threadIdx.x; bi < nbs; bi += blockDim.x) {
-      int c = kt;
+      int c = kt, c64 = kt;
       if (self_out) {
-        c = (b0 + bi >= t0 && b0 + bi < t0 + kt) ? 1 : 0;  // the item (P, P) lies in this tile
+        c = c64 = (b0 + bi >= t0 && b0 + bi < t0 + kt) ? 1 : 0;  // the item (P, P) lies in this tile
       } else if (tau > 0.0) {
         const double sb = bra[b0 + bi].pad[0];
-        if (sb * s_ket[0].pad[0] < tau) {
-          c = 0;
-        } else {
-          int lo = 1, hi = kt;  // first index with sb * S_Q < tau lies in [lo, hi]
+        // first index with sb * S_Q < thr (S_Q decreasing along the tile)
+        auto first_below = [&](double thr) {
+          int lo = 0, hi = kt;
           while (lo < hi) {
             const int mid = (lo + hi) >> 1;
-            if (sb * s_ket[mid].pad[0] < tau) hi = mid; else lo = mid + 1;
+            if (sb * s_ket[mid].pad[0] < thr) hi = mid; else lo = mid + 1;
           }
-          c = lo;
-        }
+          return lo;
+        };
+        c = first_below(tau);
+        c64 = first_below(tau32);
       }
-      s_scan[bi + 1] = c;
+      s_scan[bi + 1] = c64;
+      s_scan32[bi + 1] = c - c64;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       s_scan[0] = 0;
-      for (int bi = 0; bi < nbs; bi++) s_scan[bi + 1] += s_scan[bi];
+      s_scan32[0] = 0;
+      for (int bi = 0; bi < nbs; bi++) {
+        s_scan[bi + 1] += s_scan[bi];
+        s_scan32[bi + 1] += s_scan32[bi];
+      }
     }
     __syncthreads();
 
-    const int nitems = s_scan[nbs];
     // Without r^2-type fits each thread takes a contiguous run of items (bra-major), so its bra
     // polynomials change only when the run crosses a bra pair.  With them the items are dealt
     // round-robin (consecutive threads, consecutive ket pairs of one bra pair): the threads of a
     // warp then share their bra polynomials and the data-dependent branches of the option loops.
-    const int per_t = (nitems + (int)blockDim.x - 1) / (int)blockDim.x;
-    const int e_begin = T2 ? (int)threadIdx.x : min(nitems, (int)threadIdx.x * per_t);
-    const int e_end = T2 ? nitems : min(nitems, e_begin + per_t);
-    const int e_step = T2 ? (int)blockDim.x : 1;
-    int bcur = -1;
-    double Pn[3 * NO * (L + 1)];
-    PrimPair P;
-    for (int e = e_begin; e < e_end; e += e_step) {
-      // item e -> (bra bi, ket ik): last bi with s_scan[bi] <= e
+    // item e of a tier -> (bra bi, position in the bra's range): last bi with scan[bi] <= e
+    auto locate = [&](const int* scan, int e) {
       int lo = 0, hi = nbs - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (s_scan[mid] <= e) lo = mid; else hi = mid - 1;
+        if (scan[mid] <= e) lo = mid; else hi = mid - 1;
       }
-      const int ib = b0 + lo, ik = self_out ? ib - t0 : e - s_scan[lo];
-      if (ib != bcur) {
-        P = bra[ib];
-        bcur = ib;
-        pair_polys<L, T2>(S, 0, P, Pn);
+      return lo;
+    };
+    {  // FP64 tier
+      const int nitems = s_scan[nbs];
+      const int per_t = (nitems + (int)blockDim.x - 1) / (int)blockDim.x;
+      const int e_begin = T2 ? (int)threadIdx.x : min(nitems, (int)threadIdx.x * per_t);
+      const int e_end = T2 ? nitems : min(nitems, e_begin + per_t);
+      const int e_step = T2 ? (int)blockDim.x : 1;
+      int bcur = -1;
+      double Pn[3 * NO * (L + 1)];
+      PrimPair P;
+      for (int e = e_begin; e < e_end; e += e_step) {
+        const int bi = locate(s_scan, e);
+        const int ib = b0 + bi, ik = self_out ? ib - t0 : e - s_scan[bi];
+        if (ib != bcur) {
+          P = bra[ib];
+          bcur = ib;
+          pair_polys<L, T2, double>(S, 0, P, Pn);
+        }
+        const PrimPair& Q = s_ket[ik];
+        const double v = prim_quartet<L, TC, double>(S, view64(P), Pn, view64(Q), s_q + (size_t)ik * QW, s_boys);
+        if (self_out) {
+          self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
+          continue;
+        }
+        // the coefficient product of src/gauss_ijkl.F90:137
+        acc = fma(P.coef * Q.coef, v, acc);
       }
-      const PrimPair& Q = s_ket[ik];
-      const double v = prim_quartet<L, TC>(S, P, Pn, Q, s_q + (size_t)ik * QW, s_boys);
-      if (self_out) {
-        self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
-        continue;
+    }
+    {  // FP32 tier
+      const int nitems = s_scan32[nbs];
+      const int per_t = (nitems + (int)blockDim.x - 1) / (int)blockDim.x;
+      const int e_begin = T2 ? (int)threadIdx.x : min(nitems, (int)threadIdx.x * per_t);
+      const int e_end = T2 ? nitems : min(nitems, e_begin + per_t);
+      const int e_step = T2 ? (int)blockDim.x : 1;
+      int bcur = -1;
+      float Pn[3 * NO * (L + 1)];
+      PairView<float> Pv;
+      for (int e = e_begin; e < e_end; e += e_step) {
+        const int bi = locate(s_scan32, e);
+        const int ib = b0 + bi;
+        const int ik = (s_scan[bi + 1] - s_scan[bi]) + (e - s_scan32[bi]);
+        if (ib != bcur) {
+          const PrimPairF P = braf[ib];
+          bcur = ib;
+          pair_polys<L, T2, float>(S, 0, P, Pn);
+          Pv = view32(P);
+        }
+        acc32 += prim_quartet<L, TC, float>(S, Pv, Pn, s_ketf[ik], s_qf + (size_t)ik * QW, s_boys32);
       }
-      // the coefficient product of src/gauss_ijkl.F90:137
-      acc = fma(P.coef * Q.coef, v, acc);
     }
   }
+  acc += (double)acc32;
   // block reduction in a fixed order
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);

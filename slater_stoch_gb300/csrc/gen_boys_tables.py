@@ -10,6 +10,11 @@ exponential, computed with mpmath at 40 significant digits and rounded once to d
   term below 3e-17 relative).
 * EXP2: 2^(j/32), j = 0..31, and the Cody-Waite split of ln2/32, for the table-driven
   exponential of P. T. P. Tang (ACM TOMS 15 (1989) 144-157).
+* BOYS32 (single precision, for primitive quartets evaluated in FP32): grid T_k = k/8
+  (k = 0..240, T in [0, 30]); row k holds F_n(T_k), n = 0..21, rounded to float; the kernel
+  sums F_nf(T_k + d) = sum_{j<6} F_{nf+j}(T_k) (-d)^j / j! (|d| <= 1/16, first omitted term
+  below 1e-10 relative) and recurs downwards; beyond T = 30 the asymptotic form is exact to
+  e^-30.
 
 Run: python slater_stoch_gb300/csrc/gen_boys_tables.py  (rewrites boys_tables.cuh beside it).
 """
@@ -23,6 +28,7 @@ mp.mp.dps = 40
 
 HI_K, HI_H, HI_T0, HI_J = 281, mp.mpf(1) / 8, mp.mpf(1), 9
 LO_K, LO_H, LO_N = 17, mp.mpf(1) / 16, 25
+B32_K, B32_H, B32_N = 241, mp.mpf(1) / 8, 22
 
 
 def boys(n: int, T) -> mp.mpf:
@@ -35,11 +41,18 @@ def d(x) -> str:
     return repr(float(x))
 
 
-def table(name: str, vals, per_line: int) -> str:
+def f32(x) -> str:
+    import struct
+    v = struct.unpack("f", struct.pack("f", float(x)))[0]  # rounded to float
+    return repr(v) + "f"
+
+
+def table(name: str, vals, per_line: int, ctype: str = "double") -> str:
+    fmt = d if ctype == "double" else f32
     lines = []
     for i in range(0, len(vals), per_line):
-        lines.append("    " + ", ".join(d(v) for v in vals[i:i + per_line]) + ",")
-    return f"SS_BOYS_TAB double {name}[{len(vals)}] = {{\n" + "\n".join(lines) + "\n};\n"
+        lines.append("    " + ", ".join(fmt(v) for v in vals[i:i + per_line]) + ",")
+    return f"SS_BOYS_TAB {ctype} {name}[{len(vals)}] = {{\n" + "\n".join(lines) + "\n};\n"
 
 
 def main() -> None:
@@ -54,6 +67,11 @@ def main() -> None:
         for n in range(LO_N):
             lo.append(boys(n, T))
     e2 = [mp.power(2, mp.mpf(j) / 32) for j in range(32)]
+    b32 = []
+    for k in range(B32_K):
+        T = k * B32_H
+        for n in range(B32_N):
+            b32.append(boys(n, T))
     ln2_32 = mp.log(2) / 32
     hi_part = float(ln2_32)
     lo_part = float(ln2_32 - mp.mpf(hi_part))
@@ -74,6 +92,8 @@ def main() -> None:
         f"constexpr int BOYS_HI_J = {HI_J};       // a_j = F_j(T_k) / j!",
         f"constexpr int BOYS_LO_K = {LO_K};      // T_k = k/16",
         f"constexpr int BOYS_LO_N = {LO_N};      // F_n(T_k), n = 0..24",
+        f"constexpr int BOYS32_K = {B32_K};     // T_k = k/8, T in [0, 30]",
+        f"constexpr int BOYS32_N = {B32_N};      // F_n(T_k), n = 0..21 (float)",
         f"constexpr double EXP_INV_LN2_32 = {d(32 / mp.log(2))};  // 32/ln2",
         f"constexpr double EXP_LN2_32_HI = {d(hi_part)};  // ln2/32 = HI + LO",
         f"constexpr double EXP_LN2_32_LO = {d(lo_part)};",
@@ -81,6 +101,7 @@ def main() -> None:
         table("boys_hi_tab", hi, HI_J),
         table("boys_lo_tab", lo, 5),
         table("exp2_32_tab", e2, 4),
+        table("boys32_tab", b32, 11, "float"),
         "}  // namespace ss",
         "",
     ]

@@ -20,15 +20,15 @@ cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, c
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
-                             double* partial, double* self_out);
+                             double* partial, double* self_out, const PrimPairF* ppf);
+__global__ void prim_pair_to_f32(int64_t npp, const PrimPair* in, PrimPairF* out);
 __global__ void prim_pair_sort(const PrimPair* in, const int64_t* off, const int* cnt, PrimPair* out);
 __global__ void prim_pair_count(BasisDev B, int npairs, int* cnt);
 void jobs_shutdown(ss_ctx* c);
 __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* off, PrimPair* out);
 __global__ void eri_finalize(int64_t nint, const int32_t* is, const int32_t* js, const int32_t* ks,
-                             const int32_t* ls, const int64_t* slot, int split, const double* partial,
+                             const int32_t* ls, const int64_t* slot, const double* partial,
                              const double* pre, int n, double* out);
-__global__ void precond_finalize(int n, int split, const double* partial, double* pre);
 }  // namespace ss
 
 static thread_local std::string g_err;
@@ -125,41 +125,42 @@ static int total_pow(const ss_ctx* c, int f) {
 static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const int32_t* d_qks,
                    const int32_t* d_qls, const std::vector<int32_t>& qis, const std::vector<int32_t>& qjs,
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
-                   const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int& split_out,
+                   const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
                    const double* d_pre, double eps, double* self_out = nullptr) {
-  // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
-  // functions, 3 standing for three or four)
-  const int NB = 4 * (SS_MAX_POW + 1);
+  // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four functions)
+  const int NB = 5 * (SS_MAX_POW + 1);
   std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
     int i = qis[t] - 1, k = qks[t] - 1, j = qjs[t] - 1, l = qls[t] - 1;
     int L = std::max(pair_L(c, i, k), pair_L(c, j, l));
     int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
-    bucket[4 * L + std::min(nt, 3)].push_back(t);
+    bucket[5 * L + nt].push_back(t);
   }
-  int64_t nsel = (int64_t)sel.size();
-  // one split for all classes keeps the slot arithmetic simple; short lists (the Schwarz
-  // diagonal: n(n+1)/2 quartets, a few of them in each heavy class) are split up to 16 ways
-  const int target = c->num_sms * 32;
-  int split = (int)std::min<int64_t>(16, std::max<int64_t>(1, (target + std::max<int64_t>(nsel, 1) - 1) /
-                                                             std::max<int64_t>(nsel, 1)));
-  split_out = split;
+  // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes
+  // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 64 ways).
+  const int64_t target = (int64_t)c->num_sms * 8;
   std::vector<int64_t> work;
-  work.reserve(nsel);
-  std::vector<int64_t> begin(NB), count(NB);
-  std::vector<int> maxk(NB, 0);
+  work.reserve(sel.size());
+  std::vector<int64_t> begin(NB), count(NB), pbase(NB + 1, 0);
+  std::vector<int> maxk(NB, 0), bsplit(NB, 1);
   slot_of_sel.assign(qis.size(), -1);
   for (int bk = 0; bk < NB; bk++) {
     begin[bk] = (int64_t)work.size();
+    const int64_t cnt = (int64_t)bucket[bk].size();
+    bsplit[bk] = cnt ? (int)std::min<int64_t>(64, std::max<int64_t>(1, (target + cnt - 1) / cnt)) : 1;
+    int64_t local = 0;
     for (int64_t t : bucket[bk]) {
-      slot_of_sel[t] = (int64_t)work.size();
+      slot_of_sel[t] = ((pbase[bk] + local * bsplit[bk]) << SLOT_SPLIT_BITS) | bsplit[bk];
+      local++;
       work.push_back(t);
       int j = qjs[t] - 1, l = qls[t] - 1;
       maxk[bk] = std::max(maxk[bk], c->h_pp_cnt[ss_pair_index(j, l)]);
     }
-    count[bk] = (int64_t)work.size() - begin[bk];
+    count[bk] = cnt;
+    pbase[bk + 1] = pbase[bk] + cnt * bsplit[bk];
   }
-  int rc = dev_alloc(c, c->d_scratch_b, sizeof(double) * std::max<int64_t>(nsel * split, 1));
+  npartial = pbase[NB];
+  int rc = dev_alloc(c, c->d_scratch_b, sizeof(double) * std::max<int64_t>(npartial, 1));
   if (rc) return rc;
   if (work.empty()) return SS_OK;  // e.g. a one-function basis: its only quartet is diagonal
   rc = h2d(c, c->d_scratch_a, work.data(), sizeof(int64_t) * work.size());
@@ -168,13 +169,14 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   double* d_partial = (double*)c->d_scratch_b.ptr;
   for (int bk = 0; bk < NB; bk++) {
     if (!count[bk]) continue;
-    const int L = bk / 4;
-    const int tc = bk % 4;
+    const int L = bk / 5;
+    const int tc = bk % 5;
     const bool t2 = tc > 0;
     int ktile;
     size_t smem;
     eri_tile(L, t2, std::max(maxk[bk], 1), &ktile, &smem);
     // grid.x is limited to 2^31-1: launch in chunks of quartets
+    const int split = bsplit[bk];
     const int64_t chunk = (int64_t)(2147483647 / split);
     for (int64_t s0 = 0; s0 < count[bk]; s0 += chunk) {
       int64_t nq = std::min(chunk, count[bk] - s0);
@@ -182,8 +184,8 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
       cudaError_t e = launch_eri_class(L, tc, grid, ktile, smem, c->stream, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
-                                       d_qjs, d_qks, d_qls, d_pre, eps, d_partial + (begin[bk] + s0) * split,
-                                       self_out);
+                                       d_qjs, d_qks, d_qls, d_pre, eps, d_partial + pbase[bk] + s0 * split,
+                                       self_out, (const PrimPairF*)c->d_ppf.ptr);
       if (e != cudaSuccess) {
         ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
         return SS_ERR_CUDA;
@@ -220,6 +222,13 @@ static int sort_prim_pairs(ss_ctx* c) {
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;
   SS_CUDA_TRY(cudaMemcpyAsync(c->d_pp.ptr, p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  // FP32 copies in the same order
+  const int64_t npp = std::max<int64_t>(c->h_pp_off[npairs], 1);
+  TRY(dev_alloc(c, c->d_ppf, sizeof(PrimPairF) * npp));
+  prim_pair_to_f32<<<(unsigned)((npp + 255) / 256), 256, 0, c->stream>>>(npp, (const PrimPair*)c->d_pp.ptr,
+                                                                          (PrimPairF*)c->d_ppf.ptr);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
   return SS_OK;
 }
 
@@ -244,17 +253,17 @@ int ensure_precond(ss_ctx* c) {
   if (!rc) rc = h2d(c, dk, qk.data(), sizeof(int32_t) * np);
   std::vector<int64_t> sel(np), slot;
   std::iota(sel.begin(), sel.end(), 0);
-  int split = 1;
+  int64_t npartial = 0;
   // 1. primitive-pair Schwarz factors (items (P,P) of the diagonal quartets) into pad[0],
   // 2. per-pair sort by decreasing factor, 3. the diagonal quartets themselves
   if (!rc)
     rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
-                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split, nullptr, 0.0,
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0,
                  (double*)((char*)c->d_pp.ptr + offsetof(PrimPair, pad)));
   if (!rc) rc = sort_prim_pairs(c);
   if (!rc)
     rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
-                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, split, nullptr, 0.0);
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0);
   if (rc) {
     dev_free(c, di);
     dev_free(c, dk);
@@ -262,10 +271,10 @@ int ensure_precond(ss_ctx* c) {
   }
   // slots are a permutation of pair indices: gather partials back into pair order on the host side
   // by re-sorting (cheap: np entries)
-  std::vector<double> part((size_t)np * split);
+  std::vector<double> part((size_t)std::max<int64_t>(npartial, 1));
   rc = dev_alloc(c, c->d_precond, sizeof(double) * n * n);
   if (rc) return rc;
-  cudaError_t e = cudaMemcpyAsync(part.data(), c->d_scratch_b.ptr, sizeof(double) * np * split,
+  cudaError_t e = cudaMemcpyAsync(part.data(), c->d_scratch_b.ptr, sizeof(double) * part.size(),
                                   cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   dev_free(c, di);
@@ -277,7 +286,7 @@ int ensure_precond(ss_ctx* c) {
   c->h_precond.assign((size_t)n * n, 0.0);
   for (int64_t p = 0; p < np; p++) {
     double v = 0.0;
-    for (int t = 0; t < split; t++) v = v + part[slot[p] * split + t];
+    for (int t = 0; t < slot_split(slot[p]); t++) v = v + part[slot_offset(slot[p]) + t];
     int i = qi[p] - 1, k = qk[p] - 1;
     c->h_precond[i + (size_t)n * k] = v;
     c->h_precond[k + (size_t)n * i] = v;
@@ -311,9 +320,9 @@ int ensure_gauss(ss_ctx* c) {
   }
   c->n_removed = nzero;
   std::vector<int64_t> slot;
-  int split = 1;
+  int64_t npartial = 0;
   rc = run_eri(c, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
-               (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, split,
+               (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, npartial,
                (const double*)c->d_precond.ptr, PRIM_SCREEN_EPS);
   if (rc) return rc;
   rc = h2d(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
@@ -323,7 +332,7 @@ int ensure_gauss(ss_ctx* c) {
   int64_t nb = (c->nint + 255) / 256;
   eri_finalize<<<(unsigned)nb, 256, 0, c->stream>>>(
       c->nint, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
-      (const int32_t*)c->d_ls.ptr, (const int64_t*)c->d_scratch_c.ptr, split,
+      (const int32_t*)c->d_ls.ptr, (const int64_t*)c->d_scratch_c.ptr,
       (const double*)c->d_scratch_b.ptr, (const double*)c->d_precond.ptr, n, (double*)c->d_gauss.ptr);
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;
@@ -389,7 +398,7 @@ void ss_destroy(ss_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->d_center, &c->d_npower, &c->d_nsto, &c->d_itype, &c->d_ng, &c->d_cg, &c->d_gg,
-                    &c->d_gs, &c->d_pp, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
+                    &c->d_gs, &c->d_pp, &c->d_ppf, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
                     &c->d_ls, &c->d_precond, &c->d_gauss, &c->d_mean, &c->d_sigma, &c->d_scratch_a,
                     &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d};
   for (DevBuf* b : bufs) dev_free(c, *b);

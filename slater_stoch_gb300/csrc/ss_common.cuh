@@ -28,6 +28,17 @@ constexpr int SS_MAX_NF = 24;        // highest Boys order F_n used by one primi
 // per function pair the skipped part of an ERI is below 8.1e5 * 1e-18 = 8.1e-13 of its Schwarz
 // bound sqrt((ik|ik)(jl|jl)), and in practice far below (the bound is loose, the signs vary).
 constexpr double PRIM_SCREEN_EPS = 1e-18;
+// Where a quartet's partial sums (one per bra slice) live: slot code = offset << SLOT_SPLIT_BITS |
+// split, the partials being entries offset .. offset + split - 1 (split < 2^SLOT_SPLIT_BITS).
+constexpr int SLOT_SPLIT_BITS = 7;
+__host__ __device__ inline int64_t slot_offset(int64_t code) { return code >> SLOT_SPLIT_BITS; }
+__host__ __device__ inline int slot_split(int64_t code) { return (int)(code & ((1 << SLOT_SPLIT_BITS) - 1)); }
+// Mixed precision: a kept primitive quartet whose Schwarz bound S_P S_Q is below
+// PRIM_FP32_EPS * sqrt((ik|ik)(jl|jl)) is evaluated in FP32.  Its value is then off by at most
+// kappa * 6e-8 * S_P S_Q, kappa the cancellation amplification of its evaluation, so with 8.1e5
+// primitive quartets at most the FP32 part of an ERI is off by < kappa * 4.9e-15 of its Schwarz
+// bound: below 1e-12 of it for kappa up to 200.
+constexpr double PRIM_FP32_EPS = 1e-13;
 
 // One primitive pair of a function pair (i,k): the Gaussian product of
 // g_gauss(m1,i) and g_gauss(m2,k) (src/gaussian_product.F90:1-33), padded to 128 bytes.
@@ -41,6 +52,12 @@ struct __align__(16) PrimPair {
   double pad[3];         // [0] Schwarz factor sqrt(coef^2 (P|P)), [1] index m1*ng(k)+m2, [2] unused
 };
 static_assert(sizeof(PrimPair) == 16 * sizeof(double), "PrimPair is 16 doubles (the kernels stride by 16)");
+
+// FP32 copy of a primitive pair for the primitive quartets evaluated in FP32: fc = K_AB * coef.
+struct __align__(16) PrimPairF {
+  float p, p_inv, P[3], fc, PA[3], PB[3], pad[2];
+};
+static_assert(sizeof(PrimPairF) == 16 * sizeof(float), "PrimPairF is 16 floats");
 
 // Device view of the fitted basis (Fortran layouts, 0-based).
 struct BasisDev {

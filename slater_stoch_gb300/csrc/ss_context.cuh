@@ -59,6 +59,7 @@ struct ss_ctx {
 
   // primitive pairs
   ss::DevBuf d_pp, d_pp_off, d_pp_cnt;
+  ss::DevBuf d_ppf;  // FP32 copies of the sorted primitive pairs (mixed-precision tier)
   std::vector<int> h_pp_cnt;
   std::vector<int64_t> h_pp_off;
 

@@ -32,3 +32,12 @@ extern "C" void ss_host_exp_neg(const double* x, int count, double* out) {
   const double* e2 = tables() + ss::BOYS_HI_K * ss::BOYS_HI_J + ss::BOYS_LO_K * ss::BOYS_LO_N;
   for (int i = 0; i < count; i++) out[i] = ss::exp_neg(x[i], e2);
 }
+
+// out[i * 17 + n] = FP32 F_n(T[i]), n = 0..nf (nf <= 16)
+extern "C" void ss_host_boys32(const float* T, int count, int nf, float* out) {
+  for (int i = 0; i < count; i++) {
+    float F[17];
+    ss::boys32<16>(T[i], nf, F, ss::boys32_tab);
+    for (int n = 0; n <= 16; n++) out[i * 17 + n] = n <= nf ? F[n] : 0.f;
+  }
+}

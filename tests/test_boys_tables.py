@@ -100,3 +100,20 @@ def test_boys_upward_recursion_large_T(lib):
             assert got[t, n] == rt
             rt = (rt * di - e[t]) * two_rho_inv
             di += 2.0
+
+
+@pytest.mark.parametrize("nf", [0, 4, 9, 16])
+def test_boys32(lib, nf):
+    """FP32 Boys values (the primitive quartets evaluated in FP32): relative error within 2e-6
+    over T in [0, 60] (grid Taylor + downward recursion below 30, asymptotic form above)."""
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    lib.ss_host_boys32.argtypes = [fp, C.c_int, C.c_int, fp]
+    rng = np.random.default_rng(7 + nf)
+    T = np.concatenate([rng.uniform(0, 60, 120), [0.0, 1e-6, 0.0625, 29.99, 30.0, 30.01]]).astype(np.float32)
+    out = np.zeros(len(T) * 17, np.float32)
+    lib.ss_host_boys32(T, len(T), nf, out)
+    out = out.reshape(len(T), 17)
+    for n in range(nf + 1):
+        ref = np.array([float(_boys_mp(n, float(t))) for t in T])
+        rel = np.abs(out[:, n] - ref) / ref
+        assert rel.max() <= 2e-6, (n, rel.max(), T[rel.argmax()])
