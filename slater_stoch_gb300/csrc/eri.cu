@@ -140,11 +140,11 @@ void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
   // per ket pair: the record and its polynomials in FP64, and their FP32 copies
   const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (L + 1) + 6 * sizeof(float) +
                      sizeof(float) * 3 * no * (L + 1);
-  // Classes with r^2-type fits keep their per-item recursion tables and option polynomials in
-  // local memory: a small ket tile leaves the SM's unified L1 to them (measured on the 26-function
-  // H2O basis: 200 KB -> 40 KB tiles took these classes from 3.6 s to 2.7 s).  The other classes
-  // keep their working set in registers and take the largest tile.
-  const size_t budget = (t2 ? 40u : 168u) * 1024u;  // + ~53 KB of static tables and scans
+  // Small ket tiles: with ~53 KB of static tables and scans, 60 KB tiles let two CTAs share an
+  // SM (8 warps) and leave unified L1 to the local arrays of the classes with r^2-type fits.  On
+  // the 26-function H2O basis 168 KB (one CTA per SM) -> 60 KB tiles took the analytic stage from
+  // 2.71 to 2.53 s.
+  const size_t budget = 60u * 1024u;
   int kt = (int)(budget / per);
   kt = kt < max_cnt ? kt : max_cnt;
   kt = kt < 1 ? 1 : kt;

@@ -588,7 +588,8 @@ __global__ void __launch_bounds__(128) eri_kernel(
     // polynomials change only when the run crosses a bra pair.  With them the items are dealt
     // round-robin (consecutive threads, consecutive ket pairs of one bra pair): the threads of a
     // warp then share their bra polynomials and the data-dependent branches of the option loops.
-    // item e of a tier -> (bra bi, position in the bra's range): last bi with scan[bi] <= e
+    // A thread locates its first item once (last bi with scan[bi] <= e) and then steps: the
+    // position moves by the stride and carries over the bra pairs' range lengths.
     auto locate = [&](const int* scan, int e) {
       int lo = 0, hi = nbs - 1;
       while (lo < hi) {
@@ -606,9 +607,15 @@ __global__ void __launch_bounds__(128) eri_kernel(
       int bcur = -1;
       double Pn[3 * NO * (L + 1)];
       PrimPair P;
+      int bi = e_begin < e_end ? locate(s_scan, e_begin) : 0;
+      int pos = e_begin < e_end ? e_begin - s_scan[bi] : 0;
       for (int e = e_begin; e < e_end; e += e_step) {
-        const int bi = locate(s_scan, e);
-        const int ib = b0 + bi, ik = self_out ? ib - t0 : e - s_scan[bi];
+        while (pos >= s_scan[bi + 1] - s_scan[bi]) {
+          pos -= s_scan[bi + 1] - s_scan[bi];
+          bi++;
+        }
+        const int ib = b0 + bi, ik = self_out ? ib - t0 : pos;
+        pos += e_step;
         if (ib != bcur) {
           P = bra[ib];
           bcur = ib;
@@ -624,7 +631,7 @@ __global__ void __launch_bounds__(128) eri_kernel(
         acc = fma(P.coef * Q.coef, v, acc);
       }
     }
-    {  // FP32 tier
+    {  // FP32 tier: the ket range [c64, c) of each bra pair
       const int nitems = s_scan32[nbs];
       const int per_t = (nitems + (int)blockDim.x - 1) / (int)blockDim.x;
       const int e_begin = T2 ? (int)threadIdx.x : min(nitems, (int)threadIdx.x * per_t);
@@ -633,10 +640,16 @@ __global__ void __launch_bounds__(128) eri_kernel(
       int bcur = -1;
       float Pn[3 * NO * (L + 1)];
       PairView<float> Pv;
+      int bi = e_begin < e_end ? locate(s_scan32, e_begin) : 0;
+      int pos = e_begin < e_end ? e_begin - s_scan32[bi] : 0;
       for (int e = e_begin; e < e_end; e += e_step) {
-        const int bi = locate(s_scan32, e);
+        while (pos >= s_scan32[bi + 1] - s_scan32[bi]) {
+          pos -= s_scan32[bi + 1] - s_scan32[bi];
+          bi++;
+        }
         const int ib = b0 + bi;
-        const int ik = (s_scan[bi + 1] - s_scan[bi]) + (e - s_scan32[bi]);
+        const int ik = (s_scan[bi + 1] - s_scan[bi]) + pos;
+        pos += e_step;
         if (ib != bcur) {
           const PrimPairF P = braf[ib];
           bcur = ib;
