@@ -322,15 +322,20 @@ def main():
 
     from slater_stoch_gb300.perfmodel import primitive_quartets
     nprim = primitive_quartets(b, q)
-    flops = eri_fp64_flops(b, q)
+    from slater_stoch_gb300.perfmodel import EXEC_FLOPS
+    wl = f"{NINT_WORKLOAD}_ng20"
+    flops = eri_fp64_flops(b, q, wl)
     peak64 = fp64_peak_tflops(torch)
     achieved = flops / t_analytic / 1e12 if flops else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                 "frac": achieved / peak64 if (peak64 and achieved) else None, "traffic": None,
-                "kernel": "eri_kernel (analytic FP64 Gaussian-fit ERIs, all launches of one job)",
+                "kernel": "eri_kernel (analytic Gaussian-fit ERIs, all launches of one job)",
                 "peak_source": "measured in this run: torch float64 matmul 4096^3 (FP64 peak is not "
                                "in MEASURED_PEAKS.json)",
-                "units": f"{nprim:.4g} primitive quartets x FP64 flops per primitive quartet"}
+                "units": (f"executed FP64 flops of the job's eri_kernel launches (ncu instruction "
+                          f"counters, DFMA = 2): {flops:.4g}; plus {EXEC_FLOPS[wl][1]:.4g} FP32 FFMA flops "
+                          f"of the FP32 tier; {nprim:.4g} primitive quartets before screening")
+                if wl in EXEC_FLOPS else f"{nprim:.4g} primitive quartets x FP64 flops per primitive quartet"}
 
     if rank == 0:
         lat = sorted(times)
@@ -338,7 +343,8 @@ def main():
             "metric": METRIC,
             "value": value, "unit": "ERIs/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 analytic + bf16x3 (fp32 accumulate) MC", "data": "synthetic",
+            "dtype": ("f64 analytic (f32 for primitive quartets below 1e-13 of their Schwarz bound) + "
+                      "bf16x3 (fp32 accumulate) MC"), "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "walkers": args.walkers, "blocks": NBLOCKS, "estimator": "shared-walker, split-BF16",
                        "max_sigma_Ha": max_sigma, "sigma_target_Ha": SIGMA_TARGET,

@@ -2,19 +2,27 @@
 
 * primitive quartets: the reference loops over n_gauss(i)*nc(i) x ... x n_gauss(l)*nc(l)
   primitive Gaussian products per (ik|jl) (src/gauss_ijkl.F90:127-150), nc = 3 for the
-  r^2-type fits (i_type 2) and 1 otherwise.
-* FP64 flops per primitive quartet of the analytic stage (all eri_kernel launches of one
-  job, Schwarz diagonal included): FP64 instructions executed (DFMA counted as 2 flops,
-  DMUL/DADD as 1) divided by the primitive quartets, from an ncu capture of the H2O
-  26-function basis with 6-Gaussian fits (same kernels and angular classes as the 20-Gaussian
-  workload).  The capture command and per-class table are in profiles/eri_kernel_h2o26.md.
+  r^2-type fits (i_type 2) and 1 otherwise.  The GPU skips the primitive quartets below its
+  Schwarz screen and evaluates those below the FP32 bound in FP32, so the executed work is
+  measured rather than modelled:
+* EXEC_FLOPS: executed flops of all eri_kernel launches of one job (Schwarz factors, Schwarz
+  diagonal and screened quartets), from ncu instruction counters on the full workload
+  (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd,ffma}_pred_on.sum, one pass each; DFMA
+  and FFMA counted as 2 flops).  Command and per-class table: profiles/eri_kernel_h2o26.md.
+* EXEC_FLOPS_PER_PRIM: the earlier all-FP64 kernel's executed FP64 flops per primitive quartet
+  (241.5, unscreened), kept as the model for workloads without a measurement.
 """
 from __future__ import annotations
 
 import numpy as np
 
-# executed FP64 flops per primitive quartet of the analytic stage (ncu, see module doc)
+# executed FP64 flops per primitive quartet of the all-FP64 kernel (fallback model)
 EXEC_FLOPS_PER_PRIM = 241.5
+
+# workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job
+EXEC_FLOPS = {
+    "h2o_26_ng20": (9.5927e11, 3.9413e11),
+}
 
 
 def _pair_L(b, f1, f2):
@@ -41,6 +49,9 @@ def primitive_quartets(b, quartets) -> float:
     return float(sum(primitive_quartets_by_class(b, quartets).values()))
 
 
-def eri_fp64_flops(b, quartets) -> float:
-    """Executed FP64 flops of the analytic stage of one job."""
+def eri_fp64_flops(b, quartets, workload: str | None = None) -> float:
+    """Executed FP64 flops of the analytic stage of one job: the ncu measurement when the
+    workload has one, else the all-FP64 model."""
+    if workload in EXEC_FLOPS:
+        return EXEC_FLOPS[workload][0]
     return EXEC_FLOPS_PER_PRIM * primitive_quartets(b, quartets)
