@@ -106,6 +106,23 @@ int ss_combine(ss_ctx* ctx, double* out);
 int ss_two_e_job(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
                  int estimator, int precision, double sigma_target, double* eri, double* sigma);
 
+/* Nuclei for the one-electron nuclear attraction: xyz (3,nat) bohr, charge (nat), as the
+ * reference's centers_nuclei / charge (src/read_geometry.F90, src/common_data.F90). */
+int ss_nuclei_set(ss_ctx* ctx, int nat, const double* xyz, const double* charge);
+
+/* One-electron integrals of the Gaussian fits of the resident basis (the reference's
+ * one_e_slater loop, src/one_e_slater.F90:81-89 over src/one_elect.F90): overlap S, nuclear
+ * attraction V and kinetic K, each n x n column-major (S(i,k) = S[i + n*k]); any may be NULL. */
+int ss_one_e(ss_ctx* ctx, double* S, double* V, double* K);
+
+/* The reference's bielec_ao text output (src/two_e_slater.F90:603-613,
+ * '(4(I5,X),2D22.15)' i,j,k,l, ERI, MC error): ss_write_bielec_ao writes the context's merged
+ * ERIs and MC errors of the last job, streamed from the device in chunks;
+ * ss_write_bielec_ao_arrays writes caller arrays (sigma may be NULL: written as 0). */
+int ss_write_bielec_ao(ss_ctx* ctx, const char* path);
+int ss_write_bielec_ao_arrays(const char* path, int64_t nint, const int32_t* is, const int32_t* js,
+                              const int32_t* ks, const int32_t* ls, const double* eri, const double* sigma);
+
 /* Asynchronous job API (the reference runs one job per process and has none; these queue the
  * job of ss_two_e_job for a serving caller).  ss_job_submit copies the context's basis and
  * quartets and returns at once; the job runs on a worker thread with a private context on the

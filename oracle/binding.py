@@ -63,6 +63,8 @@ def lib():
         L.orc_pair_densities.restype = None
         L.orc_pair_densities.argtypes = [C.POINTER(OrcBasis), C.c_int, i32p, i32p, C.c_int64,
                                          f64p, f64p, f64p]
+        L.orc_one_elect.restype = None
+        L.orc_one_elect.argtypes = [C.POINTER(OrcBasis), C.c_int, f64p, f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
 
@@ -185,3 +187,14 @@ def pair_densities(ob: OracleBasis, ip, kp, u):
     rg = np.zeros((len(ip), S))
     lib().orc_pair_densities(C.byref(ob.s), len(ip), ip, kp, S, u.reshape(-1), rs, rg)
     return rs, rg
+
+
+def one_elect(ob: OracleBasis, xyz, charge):
+    """Overlap, nuclear attraction and kinetic matrices (n x n, [i, k]) of the fits
+    (src/one_elect.F90); xyz (nat, 3) bohr, charge (nat,)."""
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+    charge = np.ascontiguousarray(charge, np.float64)
+    n = ob.s.n
+    S = np.zeros(n * n); V = np.zeros(n * n); K = np.zeros(n * n)
+    lib().orc_one_elect(C.byref(ob.s), len(charge), xyz, charge, S, V, K)
+    return (S.reshape(n, n, order="F"), V.reshape(n, n, order="F"), K.reshape(n, n, order="F"))

@@ -1012,3 +1012,244 @@ int orc_zvmc_shared(const orc_basis *b, int64_t nint, const int32_t *is, const i
   free(pidx); free(pi_); free(pk_); free(s1); free(g1); free(s2); free(g2); free(e); free(acc); free(acc2);
   return 0;
 }
+
+/* ======================================================================================
+ * One-electron integrals of the Gaussian fits (src/one_e_slater.F90:81-89 and one_elect.F90)
+ * ====================================================================================== */
+
+/* src/doublefact.F90:1-14 (1 for n <= 2) */
+static double doublefact(int n) {
+  if (n <= 2) return 1.0;
+  double d = 1.0;
+  for (int i = n; i >= 1; i -= 2) d = d * (double)i;
+  return d;
+}
+
+/* src/binom.F90 (i >= 0 branch) */
+static double binom_i(int i, int j) { return fact(i) / (fact(j) * fact(i - j)); }
+
+/* src/one_electron_I.F90:1-29 */
+static double one_electron_I(int na, double ra, int nb, double rb, double gam, double rp) {
+  double rint = 0.0;
+  for (int kx = 0; kx <= na; kx++)
+    for (int lx = 0; lx <= nb; lx++) {
+      int kbig = na + nb - kx - lx;
+      if (kbig % 2 == 1) continue;
+      kbig = kbig / 2;
+      double f3 = doublefact(2 * kbig - 1);
+      double f2 = powi(1.0 / (2.0 * gam), kbig);
+      rint = rint + f2 * f3 * binom_i(na, kx) * binom_i(nb, lx) * powi(rp - ra, kx) * powi(rp - rb, lx);
+    }
+  return sqrt(M_PI / gam) * rint;
+}
+
+/* src/one_electron_sij.F90:19-54 */
+static double one_electron_Sij(const int *na, const double *ra, double gamA, const int *nb, const double *rb,
+                               double gamB) {
+  double gamtot = gamA + gamB;
+  double rmu = gamA * gamB / gamtot;
+  double rp[3];
+  for (int l = 0; l < 3; l++) rp[l] = (gamA * ra[l] + gamB * rb[l]) / gamtot;
+  double x = ra[0] - rb[0], y = ra[1] - rb[1], z = ra[2] - rb[2];
+  double AmB = x * x + y * y + z * z;
+  double arg = rmu * AmB;
+  if (arg > -log(1.e-15)) return 0.0;
+  double s = 1.0;
+  for (int l = 0; l < 3; l++) s = s * one_electron_I(na[l], ra[l], nb[l], rb[l], gamtot, rp[l]);
+  return exp(-arg) * s;
+}
+
+/* src/one_electron_Kij.F90:1-46 */
+static double one_electron_Kij(const int *na, const double *ra, double gamA, const int *nb, const double *rb,
+                               double gamB) {
+  int na2[3];
+  double sab = one_electron_Sij(na, ra, gamA, nb, rb, gamB);
+  double term1 = gamA * (3.0 + 2.0 * (na[0] + na[1] + na[2])) * sab;
+  double sab_2 = 0.0;
+  for (int l = 0; l < 3; l++) {
+    for (int li = 0; li < 3; li++) na2[li] = na[li] + (li == l ? 2 : 0);
+    sab_2 = sab_2 + one_electron_Sij(na2, ra, gamA, nb, rb, gamB);
+  }
+  double term2 = -2.0 * gamA * gamA * sab_2;
+  double sab_12 = 0.0;
+  for (int l = 0; l < 3; l++) {
+    for (int li = 0; li < 3; li++) na2[li] = (li == l && na[li] >= 2) ? na[li] - 2 : na[li];
+    sab_12 = sab_12 + na[l] * (na[l] - 1) * one_electron_Sij(na2, ra, gamA, nb, rb, gamB);
+  }
+  double term3 = -0.5 * sab_12;
+  return term1 + term2 + term3;
+}
+
+#define NAI_DIM 512
+
+/* src/multiply_poly_2.F90:1-31: d += b * c, degree nd tracked */
+static void multiply_poly_2(const double *b, int nb, const double *c, int nc, double *d, int *nd) {
+  if (nc == -1 || nb == -1) return;
+  int ndtmp = nb + nc;
+  for (int ib = 0; ib <= nb; ib++) {
+    if (b[ib] == 0.0) continue;
+    for (int ic = 0; ic <= nc; ic++) d[ib + ic] = d[ib + ic] + c[ic] * b[ib];
+  }
+  ndtmp = ndtmp > *nd ? ndtmp : *nd;
+  for (; ndtmp >= 0; ndtmp--)
+    if (d[ndtmp] != 0.0) break;
+  *nd = ndtmp;
+}
+
+static void I_x2_pol_mult_mono_elec(int c, const double *R1x, const double *R1xp, const double *R2x, double *d,
+                                    int *nd);
+
+/* src/I_x1_pol_mult_mono_elec.F90 (recursive, as the reference) */
+static void I_x1_pol_mult_mono_elec(int a, int c, const double *R1x, const double *R1xp, const double *R2x,
+                                    double *d, int *nd) {
+  double X[NAI_DIM + 1], Y[NAI_DIM + 1];
+  int nx, ny;
+  if (a == 0 && c == 0) {
+    *nd = 0;
+    d[0] = 1.0;
+    return;
+  } else if (c < 0 || *nd < 0) {
+    *nd = -1;
+    return;
+  } else if (a == 0 && c != 0) {
+    I_x2_pol_mult_mono_elec(c, R1x, R1xp, R2x, d, nd);
+  } else if (a == 1) {
+    nx = *nd;
+    for (int ix = 0; ix <= NAI_DIM; ix++) X[ix] = Y[ix] = 0.0;
+    I_x2_pol_mult_mono_elec(c - 1, R1x, R1xp, R2x, X, &nx);
+    for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * c;
+    multiply_poly_2(X, nx, R2x, 2, d, nd);
+    ny = 0;
+    I_x2_pol_mult_mono_elec(c, R1x, R1xp, R2x, Y, &ny);
+    multiply_poly_2(Y, ny, R1x, 2, d, nd);
+  } else {
+    for (int ix = 0; ix <= NAI_DIM; ix++) X[ix] = Y[ix] = 0.0;
+    nx = 0;
+    I_x1_pol_mult_mono_elec(a - 2, c, R1x, R1xp, R2x, X, &nx);
+    for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (a - 1);
+    multiply_poly_2(X, nx, R2x, 2, d, nd);
+    nx = *nd;
+    for (int ix = 0; ix <= NAI_DIM; ix++) X[ix] = 0.0;
+    I_x1_pol_mult_mono_elec(a - 1, c - 1, R1x, R1xp, R2x, X, &nx);
+    for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * c;
+    multiply_poly_2(X, nx, R2x, 2, d, nd);
+    ny = 0;
+    I_x1_pol_mult_mono_elec(a - 1, c, R1x, R1xp, R2x, Y, &ny);
+    multiply_poly_2(Y, ny, R1x, 2, d, nd);
+  }
+}
+
+/* src/I_x2_pol_mult_mono_elec.F90 */
+static void I_x2_pol_mult_mono_elec(int c, const double *R1x, const double *R1xp, const double *R2x, double *d,
+                                    int *nd) {
+  double X[NAI_DIM + 1], Y[NAI_DIM + 1];
+  int nx, ny;
+  if (c == 0) {
+    *nd = 0;
+    d[0] = 1.0;
+    return;
+  } else if (*nd < 0 || c < 0) {
+    *nd = -1;
+    return;
+  }
+  for (int ix = 0; ix <= NAI_DIM; ix++) X[ix] = Y[ix] = 0.0;
+  nx = 0;
+  I_x1_pol_mult_mono_elec(0, c - 2, R1x, R1xp, R2x, X, &nx);
+  for (int ix = 0; ix <= nx; ix++) X[ix] = X[ix] * (c - 1);
+  multiply_poly_2(X, nx, R2x, 2, d, nd);
+  ny = 0;
+  for (int ix = 0; ix <= NAI_DIM; ix++) Y[ix] = 0.0;
+  I_x1_pol_mult_mono_elec(0, c - 1, R1x, R1xp, R2x, Y, &ny);
+  if (ny >= 0) multiply_poly_2(Y, ny, R1xp, 2, d, nd);
+}
+
+/* src/give_polynom_mult_center_mono_elec.F90: d = Ix * Iy * Iz (polynomial in t) */
+static void give_polynom_mult_center_mono_elec(const double *A, const double *B, double alpha, double beta,
+                                               const int *pA, const int *pB, const double *C, double *d,
+                                               int *n_pt_out) {
+  double d1[NAI_DIM + 1], d2[NAI_DIM + 1], d3[NAI_DIM + 1];
+  double p = alpha + beta, p_inv = 1.0 / p, p_inv_2 = 0.5 / p, P[3];
+  for (int i = 0; i < 3; i++) P[i] = (alpha * A[i] + beta * B[i]) * p_inv;
+  double R2x[3] = {p_inv_2, 0.0, -p_inv_2};
+  for (int i = 0; i <= NAI_DIM; i++) d[i] = d1[i] = d2[i] = d3[i] = 0.0;
+  double *dd[3] = {d1, d2, d3};
+  int npt[3];
+  for (int ax = 0; ax < 3; ax++) {
+    double R1x[3] = {P[ax] - A[ax], 0.0, -(P[ax] - C[ax])};
+    double R1xp[3] = {P[ax] - B[ax], 0.0, -(P[ax] - C[ax])};
+    npt[ax] = NAI_DIM;
+    I_x1_pol_mult_mono_elec(pA[ax], pB[ax], R1x, R1xp, R2x, dd[ax], &npt[ax]);
+    if (npt[ax] < 0) {
+      *n_pt_out = -1;
+      for (int i = 0; i <= NAI_DIM; i++) d[i] = 0.0;
+      return;
+    }
+  }
+  int n_pt_tmp = 0;
+  multiply_poly_2(d1, npt[0], d2, npt[1], d, &n_pt_tmp);
+  for (int i = 0; i <= n_pt_tmp; i++) d1[i] = 0.0;
+  int nout = 0;
+  multiply_poly_2(d, n_pt_tmp, d3, npt[2], d1, &nout);
+  for (int i = 0; i <= nout; i++) d[i] = d1[i];
+  *n_pt_out = nout;
+}
+
+/* src/NAI_pol_mult.F90:1-60 */
+static double NAI_pol_mult(const double *A, const double *B, const int *pA, const int *pB, double alpha,
+                           double beta, const double *C) {
+  double two_pi = 2.0 * acos(-1.0);
+  double p = alpha + beta, p_inv = 1.0 / p, rho = alpha * beta * p_inv, dist = 0.0, dist_integral = 0.0, P[3];
+  for (int i = 0; i < 3; i++) {
+    P[i] = (alpha * A[i] + beta * B[i]) * p_inv;
+    dist = dist + (A[i] - B[i]) * (A[i] - B[i]);
+    dist_integral = dist_integral + (P[i] - C[i]) * (P[i] - C[i]);
+  }
+  double const_factor = dist * rho;
+  double cst = p * dist_integral;
+  double factor = exp(-const_factor);
+  double coeff = two_pi * factor * p_inv;
+  int n_pt = 2 * ((pA[0] + pB[0]) + (pA[1] + pB[1]) + (pA[2] + pB[2]));
+  if (n_pt == 0) return coeff * orc_rint(0, cst);
+  double d[NAI_DIM + 1];
+  int n_pt_out;
+  give_polynom_mult_center_mono_elec(A, B, alpha, beta, pA, pB, C, d, &n_pt_out);
+  if (n_pt_out < 0) return 0.0;
+  double accu = 0.0;
+  for (int i = 0; i <= n_pt_out; i += 2) {
+    if (fabs(d[i]) < 1.e-9) continue;
+    accu = accu + d[i] * orc_rint(i / 2, cst);
+  }
+  return accu * coeff;
+}
+
+/* src/one_elect.F90:1-105 for all (i,k); S, V, K column-major n x n (X[i + n*k]);
+ * nuclei: xyz[3*kn], charge[kn] (src/one_electron_Vij.F90) */
+void orc_one_elect(const orc_basis *b, int nat, const double *xyz, const double *charge, double *S, double *V,
+                   double *K) {
+  init_tables();
+  const int n = b->n;
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < n; k++) {
+      int orb[2] = {i, k};
+      int nc[2], n_c[2][4][3], ct[2][4];
+      for (int kk = 0; kk < 2; kk++) nc[kk] = components(b, orb[kk], n_c[kk], ct[kk]);
+      const double *A = b->center + 3 * i, *B = b->center + 3 * k;
+      double s = 0.0, v = 0.0, kin = 0.0;
+      for (int i1 = 0; i1 < b->n_gauss[i]; i1++)
+        for (int i2 = 0; i2 < b->n_gauss[k]; i2++)
+          for (int ii1 = 0; ii1 < nc[0]; ii1++)
+            for (int ii2 = 0; ii2 < nc[1]; ii2++) {
+              double dd = CG(b, i1, i, ct[0][ii1]) * CG(b, i2, k, ct[1][ii2]);
+              double ga = GG(b, i1, i), gb = GG(b, i2, k);
+              s = s + dd * one_electron_Sij(n_c[0][ii1], A, ga, n_c[1][ii2], B, gb);
+              double ac = 0.0;
+              for (int kn = 0; kn < nat; kn++)
+                ac = ac - charge[kn] * NAI_pol_mult(A, B, n_c[0][ii1], n_c[1][ii2], ga, gb, xyz + 3 * kn);
+              v = v + dd * ac;
+              kin = kin + dd * one_electron_Kij(n_c[0][ii1], A, ga, n_c[1][ii2], B, gb);
+            }
+      S[i + (int64_t)n * k] = s;
+      V[i + (int64_t)n * k] = v;
+      K[i + (int64_t)n * k] = kin;
+    }
+}

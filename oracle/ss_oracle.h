@@ -101,6 +101,13 @@ int orc_zvmc_shared(const orc_basis *b, int64_t nint, const int32_t *is, const i
 void orc_pair_densities(const orc_basis *b, int npairs, const int *ip, const int *kp,
                         int64_t S, const double *u, double *rhoS, double *rhoG);
 
+/* One-electron integrals of the Gaussian fits for every (i,k) (src/one_elect.F90, with
+ * one_electron_sij.F90, one_electron_Kij.F90, one_electron_Vij.F90, NAI_pol_mult.F90):
+ * overlap S, nuclear attraction V (nuclei xyz[3*nat] bohr, charge[nat]) and kinetic K,
+ * column-major n x n (X[i + n*k]). */
+void orc_one_elect(const orc_basis *b, int nat, const double *xyz, const double *charge, double *S, double *V,
+                   double *K);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,10 @@ SIGNATURES = {
                                 C.c_double, C.c_void_p]),
     "ss_job_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "ss_job_result": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "ss_nuclei_set": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p]),
+    "ss_one_e": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ss_write_bielec_ao": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ss_write_bielec_ao_arrays": (C.c_int, [C.c_char_p, C.c_int64, i32p, i32p, i32p, i32p, f64p, C.c_void_p]),
     "ss_invalidate": (C.c_int, [C.c_void_p]),
     "ss_mc_max_sigma": (C.c_double, [C.c_void_p]),
     "ss_mc_blocks_done": (C.c_int, [C.c_void_p]),

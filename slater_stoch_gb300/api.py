@@ -137,6 +137,26 @@ class Context:
                                         float(sigma_target), _ptr(eri), _ptr(sig)))
         return eri, sig
 
+    # -- one-electron integrals -----------------------------------------------------
+    def set_nuclei(self, xyz, charge):
+        """Nuclei for the nuclear attraction: xyz (nat, 3) bohr, charge (nat,)."""
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+        charge = np.ascontiguousarray(charge, np.float64).reshape(-1)
+        _lib.check(self._L.ss_nuclei_set(self._h, len(charge), xyz, charge))
+
+    def one_e(self):
+        """Overlap, nuclear attraction and kinetic matrices (n x n, [i, k]) of the fits
+        (src/one_e_slater.F90)."""
+        n = self.n
+        S = np.zeros(n * n); V = np.zeros(n * n); K = np.zeros(n * n)
+        _lib.check(self._L.ss_one_e(self._h, _ptr(S), _ptr(V), _ptr(K)))
+        return S.reshape(n, n, order="F"), V.reshape(n, n, order="F"), K.reshape(n, n, order="F")
+
+    # -- output ----------------------------------------------------------------------
+    def write_bielec_ao(self, path):
+        """The reference's bielec_ao text file of the last job's merged ERIs and MC errors."""
+        _lib.check(self._L.ss_write_bielec_ao(self._h, str(path).encode()))
+
     # -- asynchronous jobs -----------------------------------------------------------
     def job_submit(self, a_zv: float, seed: int, npts: int, nblocks: int, estimator: str = "shared",
                    precision: str = "split_bf16", sigma_target: float = 0.0) -> int:
@@ -212,3 +232,12 @@ class Context:
         _lib.check(self._L.ss_davidson(self._h, moy, LAYOUTS[layout], int(m), float(tol), int(max_iter),
                                        _ptr(ev), _ptr(vec)))
         return ev, vec.T
+
+
+def write_bielec_ao_arrays(path, quartets, eri, sigma=None):
+    """bielec_ao text file of caller arrays, written by the library (no device needed)."""
+    L = _lib.load()
+    q = [np.ascontiguousarray(x, np.int32) for x in quartets]
+    eri = np.ascontiguousarray(eri, np.float64)
+    sig = None if sigma is None else np.ascontiguousarray(sigma, np.float64)
+    _lib.check(L.ss_write_bielec_ao_arrays(str(path).encode(), len(eri), *q, eri, _ptr(sig)))

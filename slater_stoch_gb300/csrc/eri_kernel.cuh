@@ -486,7 +486,7 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
 // TC: how many of the four functions are r^2-type fits (3 cartesian components sharing
 // exponents), 0..4.
 template <int L, int TC>
-__global__ void __launch_bounds__(128) eri_kernel(
+__global__ void __launch_bounds__(128, 1) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
     const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,

@@ -57,6 +57,9 @@ struct ss_ctx {
   ss::DevBuf d_center, d_npower, d_nsto, d_itype, d_ng, d_cg, d_gg, d_gs;
   ss::BasisDev basis{};
 
+  // nuclei for the one-electron nuclear attraction (ss_nuclei_set)
+  std::vector<double> h_nuc_xyz, h_nuc_charge;
+
   // primitive pairs
   ss::DevBuf d_pp, d_pp_off, d_pp_cnt;
   ss::DevBuf d_ppf;  // FP32 copies of the sorted primitive pairs (mixed-precision tier)

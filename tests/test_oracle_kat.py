@@ -176,3 +176,36 @@ def test_davidson_oracle():
     H = A @ A.T + np.diag(np.arange(60.0))
     ev, X = OC.davidson(H, 4, tol=1e-10)
     np.testing.assert_allclose(ev, np.linalg.eigvalsh(H)[:4], rtol=1e-8)
+
+
+@pytest.mark.parametrize("zeta", [1.0, 1.7])
+def test_one_electron_sto_1s_known_answers(zeta):
+    """One-electron integrals of the 20-Gaussian fit of an unnormalised 1s STO e^(-zeta r) on a
+    unit charge at its centre (src/one_elect.F90): S = pi/zeta^3, V = -pi/zeta^2,
+    K = pi/(2 zeta), reproduced to the fit's accuracy."""
+    mol = basis.molecule_bohr(["H"], [[0.0, 0.0, 0.0]])
+    b = basis.build_basis(mol, {1: [("1S", zeta)]}, basis.FitParams(ng0=20))
+    S, V, K = O.one_elect(O.OracleBasis(b), mol.coords, mol.charges)
+    assert abs(S[0, 0] - math.pi / zeta ** 3) <= 1e-10 * math.pi / zeta ** 3
+    assert abs(V[0, 0] + math.pi / zeta ** 2) <= 1e-7 * math.pi / zeta ** 2
+    assert abs(K[0, 0] - math.pi / (2 * zeta)) <= 1e-7 * math.pi / (2 * zeta)
+
+
+def test_one_electron_gaussian_closed_forms():
+    """Two s Gaussians c e^(-a r^2) at distance R (one-Gaussian fits): overlap, kinetic and the
+    attraction of a unit charge at the first centre against their closed forms."""
+    mol = basis.molecule_bohr(["H", "H"], [[0.0, 0.0, 0.0], [0.0, 0.3, 0.9]])
+    b = basis.build_basis(mol, {1: [("1S", 1.3)]}, basis.FitParams(ng0=1))
+    ob = O.OracleBasis(b)
+    S, V, K = O.one_elect(ob, mol.coords[:1], [1.0])
+    a = b.g_gauss[0, 0]; c = b.c_gauss[0, 0, 0]
+    R2 = 0.09 + 0.81
+    p = 2 * a; mu = a * a / p
+    s_ref = c * c * (math.pi / p) ** 1.5 * math.exp(-mu * R2)
+    k_ref = mu * (3 - 2 * mu * R2) * s_ref
+    T = p * (R2 / 4)  # P is the midpoint; the charge sits at the first centre
+    f0 = 0.5 * math.sqrt(math.pi / T) * math.erf(math.sqrt(T))
+    v_ref = -c * c * 2 * math.pi / p * math.exp(-mu * R2) * f0
+    assert abs(S[0, 1] - s_ref) <= 1e-13 * s_ref
+    assert abs(K[0, 1] - k_ref) <= 1e-12 * abs(k_ref)
+    assert abs(V[0, 1] - v_ref) <= 1e-12 * abs(v_ref)
