@@ -133,3 +133,18 @@ def test_bielec_ao_round_trip(tmp_path):
     assert len(line) == 4 * 6 + 2 * 22
     chunks = list(trexio_chunks(q, v))
     assert sum(len(c[2]) for c in chunks) == int(np.sum(np.abs(v) >= 1e-15))
+
+
+def test_library_bielec_ao_writer_matches_fortran_format(tmp_path):
+    """The library's bielec_ao writer (no device involved) produces the same bytes as the
+    Fortran-format reference implementation of '(4(I5,X),2D22.15)' in output.py."""
+    from slater_stoch_gb300 import api, output
+    rng = np.random.default_rng(4)
+    q = basis.build_mapping(5)
+    nint = len(q[0])
+    v = rng.standard_normal(nint) * 10.0 ** rng.integers(-120, 3, nint)
+    v[:4] = [0.0, -1.0, 1.0e-100, -9.99999999999999999e-16]
+    s = np.abs(rng.standard_normal(nint)) * 1e-7
+    api.write_bielec_ao_arrays(tmp_path / "lib.txt", q, v, s)
+    output.write_bielec_ao(tmp_path / "py.txt", q, v, s)
+    assert (tmp_path / "lib.txt").read_bytes() == (tmp_path / "py.txt").read_bytes()
