@@ -223,6 +223,15 @@ class Context:
         _lib.check(self._L.ss_psd_project(self._h, moy, LAYOUTS[layout], _ptr(nrem)))
         return moy, int(nrem[0])
 
+    def davidson_clean(self, moy, layout: str = "ref_n2", block: int = 0, max_blocks: int = 0,
+                       tol: float = 1e-8, max_iter: int = 2000):
+        """Matrix-free removal of negative eigencomponents (davidson_clean's nbasis >= 200 path)."""
+        moy = np.array(moy, dtype=np.float64, copy=True)
+        nrem = np.zeros(1, np.int32)
+        _lib.check(self._L.ss_davidson_clean(self._h, moy, LAYOUTS[layout], int(block), int(max_blocks),
+                                             float(tol), int(max_iter), _ptr(nrem)))
+        return moy, int(nrem[0])
+
     def davidson(self, moy, m: int = 10, layout: str = "packed_pair", tol: float = 1e-8,
                  max_iter: int = 200):
         moy = np.ascontiguousarray(moy, np.float64)

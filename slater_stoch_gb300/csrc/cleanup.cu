@@ -590,6 +590,272 @@ int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, i
   return SS_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// Matrix-free Davidson cleanup (the nbasis >= 200 branch of src/davidson_clean.F90:120-323)
+// ---------------------------------------------------------------------------------------
+// The ERI matrix is never formed.  Each pass writes the quartet list once into the packed
+// lower triangle of the pair metric, tri[P1 (P1+1)/2 + P2] = (ik|jl) with P1 = pair(i,k) >=
+// P2 = pair(j,l): one double per canonical quartet, the reference's 8-fold list without its
+// n^2 x n^2 expansion.  Both layouts read their elements from it: PACKED_PAIR M(p, q) =
+// tri(max, min); REF_N2 W(a + b n, c + d n) = <ab|cd> = (ac|bd) = M(pair(a,c), pair(b,d)) --
+// the same element the reference's 8 index permutations of one quartet reach
+// (src/davidson_clean.F90:165-187).  Products H X are gathered row by row, so they carry no
+// atomics and are reproducible.
+__device__ __forceinline__ int64_t sym_pair(int64_t a, int64_t b) {
+  return a >= b ? a * (a + 1) / 2 + b : b * (b + 1) / 2 + a;
+}
+
+__global__ void tri_fill_kernel(int64_t nint, const int32_t* __restrict__ is, const int32_t* __restrict__ js,
+                                const int32_t* __restrict__ ks, const int32_t* __restrict__ ls,
+                                const double* __restrict__ moy, double* __restrict__ tri) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int i = is[q] - 1, j = js[q] - 1, k = ks[q] - 1, l = ls[q] - 1;
+  tri[sym_pair(sym_pair(i, k), sym_pair(j, l))] = moy[q];
+}
+
+__device__ __forceinline__ double op_element(int layout, int n, const double* __restrict__ tri, int r, int c) {
+  if (layout == SS_LAYOUT_REF_N2) {
+    const int a = r % n, b = r / n, cc = c % n, d = c / n;
+    return tri[sym_pair(sym_pair(a, cc), sym_pair(b, d))];
+  }
+  return tri[sym_pair(r, c)];
+}
+
+constexpr int MF_ROWS = 16, MF_COLS = 32, MF_MAXM = 128;
+
+// Y = H X, X and Y N x m column-major (leading dimension N), m <= MF_MAXM.  One CTA per 16
+// rows; thread t owns row t % 16 and the columns t / 16 + 16 s.
+__global__ void __launch_bounds__(256) op_apply_kernel(int layout, int n, int N, int m,
+                                                       const double* __restrict__ tri,
+                                                       const double* __restrict__ X, double* __restrict__ Y) {
+  __shared__ double sE[MF_ROWS][MF_COLS + 1];
+  __shared__ double sX[MF_COLS][MF_MAXM];
+  const int r0 = blockIdx.x * MF_ROWS;
+  const int t = threadIdx.x, rr = t & (MF_ROWS - 1), c16 = t >> 4;
+  double acc[MF_MAXM / 16];
+#pragma unroll
+  for (int s = 0; s < MF_MAXM / 16; s++) acc[s] = 0.0;
+  for (int c0 = 0; c0 < N; c0 += MF_COLS) {
+    for (int e = t; e < MF_ROWS * MF_COLS; e += blockDim.x) {
+      const int er = e / MF_COLS, ec = e % MF_COLS;
+      sE[er][ec] = (r0 + er < N && c0 + ec < N) ? op_element(layout, n, tri, r0 + er, c0 + ec) : 0.0;
+    }
+    for (int e = t; e < MF_COLS * m; e += blockDim.x) {
+      const int ec = e % MF_COLS, j = e / MF_COLS;
+      sX[ec][j] = (c0 + ec < N) ? X[(c0 + ec) + (size_t)j * N] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int cc = 0; cc < MF_COLS; cc++) {
+      const double h = sE[rr][cc];
+#pragma unroll
+      for (int s = 0; s < MF_MAXM / 16; s++)
+        if (c16 + 16 * s < m) acc[s] = fma(h, sX[cc][c16 + 16 * s], acc[s]);
+    }
+    __syncthreads();
+  }
+  if (r0 + rr < N) {
+#pragma unroll
+    for (int s = 0; s < MF_MAXM / 16; s++)
+      if (c16 + 16 * s < m) Y[(r0 + rr) + (size_t)(c16 + 16 * s) * N] = acc[s];
+  }
+}
+
+// lowest m eigenvectors of the k x k projected matrix (row-major, eigenvectors as columns)
+// into V (k x m column-major)
+__global__ void ritz_cols_kernel(int k, int m, const double* __restrict__ A, double* __restrict__ V) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)k * m) return;
+  const int i = (int)(e % k), j = (int)(e / k);
+  V[e] = A[(size_t)i * k + j];
+}
+
+// residuals R_j = E_j X_j - (H X)_j (src/davidson_clean.F90:277-283)
+__global__ void residual_kernel(int N, int m, const double* __restrict__ X, const double* __restrict__ WX,
+                                const double* __restrict__ E, double* __restrict__ R) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)N * m) return;
+  R[e] = E[e / N] * X[e] - WX[e];
+}
+
+// moy(kcp) -= E_j U(ii, j) U(jj, j) for the nneg negative pairs, canonical (ii, jj) of each
+// quartet (src/davidson_clean.F90:310-317)
+__global__ void deflate_kernel(int64_t nint, int layout, int n, int N, const int32_t* __restrict__ is,
+                               const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
+                               const int32_t* __restrict__ ls, int nneg, const double* __restrict__ E,
+                               const double* __restrict__ U, double* __restrict__ moy) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nint) return;
+  const int i = is[q] - 1, j = js[q] - 1, k = ks[q] - 1, l = ls[q] - 1;
+  int64_t ii, jj;
+  if (layout == SS_LAYOUT_REF_N2) {
+    ii = i + (int64_t)j * n;
+    jj = k + (int64_t)l * n;
+  } else {
+    ii = sym_pair(i, k);
+    jj = sym_pair(j, l);
+  }
+  double v = moy[q];
+  for (int t = 0; t < nneg; t++) v = v - E[t] * U[ii + (size_t)t * N] * U[jj + (size_t)t * N];
+  moy[q] = v;
+}
+
+static int op_apply(ss_ctx* c, int layout, int N, int m, const double* tri, const double* X, double* Y) {
+  op_apply_kernel<<<(N + MF_ROWS - 1) / MF_ROWS, 256, 0, c->stream>>>(layout, c->n, N, m, tri, X, Y);
+  SS_CUDA_TRY(cudaGetLastError());
+  c->launches++;
+  return SS_OK;
+}
+
+// V (N x b, leading dimension N) made orthonormal and orthogonal to U (N x k): two classical
+// Gram-Schmidt passes against U, Householder QR of the block, then the pair once more (a block
+// whose residuals vanished comes back from the first QR with unit columns that need not be
+// orthogonal to U).
+static int orthonormalize_block(ss_ctx* c, cublasHandle_t hb, int N, int k, int b, const double* U, double* V,
+                                double* tmp, double* Qw, double* tau) {
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  for (int round = 0; round < 2; round++) {
+    for (int rep = 0; rep < 2 && k > 0; rep++) {
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, b, N, &one, U, N, V, N, &zero, tmp, k));
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, b, k, &mone, U, N, tmp, k, &one, V, N));
+    }
+    TRY(ortho_qr(c->stream, N, b, V, N, Qw, tau, &c->launches));
+  }
+  return SS_OK;
+}
+
+// Block Davidson for the lowest `m` eigenpairs (the reference's mmax = NMAX = nbasis unless
+// given), plain residual expansion, basis of at most kmax = nmax m vectors (capped at N and at
+// the 1024 of the device eigensolver) restarted from the Ritz vectors when full.  A search ends
+// when the Ritz pairs up to the middle one (index m/2, the reference's test,
+// src/davidson_clean.F90:286) and every negative Ritz pair have residual norm below tol, or
+// when the basis spans the whole space; its negative Ritz pairs (below -1e-13 of the largest
+// |ERI|, rounding level) are then deflated from moy and the search restarts from new random
+// vectors, until a search finds none.  The reference also ends a search as soon as all m Ritz
+// values are negative and deflates those pairs unconverged; converging them first makes the
+// result with a basis that can span the whole space the exact projection's (for the packed
+// metric, whose canonical read-back is exact).  The basis is kept orthonormal, so the
+// projected problem is a standard symmetric one (the reference solves the equivalent
+// generalized problem with dsygv).
+int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, double tol, int max_iter,
+                   int* n_removed) {
+  const int n = c->n;
+  const int64_t N64 = layout == SS_LAYOUT_REF_N2 ? (int64_t)n * n : (int64_t)n * (n + 1) / 2;
+  if (N64 < 2 || N64 > (1 << 26)) {
+    ss_set_error_msg("davidson_clean: matrix dimension %lld out of range", (long long)N64);
+    return SS_ERR_ARG;
+  }
+  const int N = (int)N64;
+  if (m <= 0) m = n;  // src/davidson_clean.F90:129-131: mmax = NMAX = nbasis
+  if (nmax <= 0) nmax = n;
+  m = std::min(m, std::max(1, N / 2));
+  if (m > MF_MAXM) {
+    ss_set_error_msg("davidson_clean: block of %d vectors above the %d supported", m, MF_MAXM);
+    return SS_ERR_UNSUPPORTED;
+  }
+  int kmax = (int)std::min<int64_t>({(int64_t)m * std::max(nmax, 2), (int64_t)N, 1024});
+  kmax = kmax / m * m;
+  if (kmax < 2 * m) kmax = 2 * m;  // m <= N/2 and m <= 128: 2m <= min(N, 1024)
+  double scale = 0.0;
+  for (int64_t q = 0; q < c->nint; q++) scale = std::max(scale, fabs(moy_host[q]));
+  const double neg_eps = 1e-13 * scale;
+  cublasHandle_t hb;
+  TRY(get_cublas(c, &hb));
+  void* p;
+  double *tri, *U, *WU, *S, *Sa, *ev, *ework, *X, *WX, *R, *nrm, *tmp, *moy, *Qw, *tau;
+  int* info;
+  const int64_t T = (int64_t)(n * (n + 1) / 2) * (n * (n + 1) / 2 + 1) / 2;
+  const size_t Nk = (size_t)N * kmax, Nm = (size_t)N * m;
+  TRY(pool_get(c, "dc_tri", sizeof(double) * T, &p)); tri = (double*)p;
+  TRY(pool_get(c, "dc_U", sizeof(double) * Nk, &p)); U = (double*)p;
+  TRY(pool_get(c, "dc_WU", sizeof(double) * Nk, &p)); WU = (double*)p;
+  TRY(pool_get(c, "dc_S", sizeof(double) * kmax * kmax, &p)); S = (double*)p;
+  TRY(pool_get(c, "dc_Sa", sizeof(double) * kmax * kmax, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dc_ev", sizeof(double) * kmax, &p)); ev = (double*)p;
+  TRY(pool_get(c, "dc_ework", sizeof(double) * 2 * kmax, &p)); ework = (double*)p;
+  TRY(pool_get(c, "dc_X", sizeof(double) * Nm, &p)); X = (double*)p;
+  TRY(pool_get(c, "dc_WX", sizeof(double) * Nm, &p)); WX = (double*)p;
+  TRY(pool_get(c, "dc_R", sizeof(double) * Nm, &p)); R = (double*)p;
+  TRY(pool_get(c, "dc_nrm", sizeof(double) * m, &p)); nrm = (double*)p;
+  TRY(pool_get(c, "dc_tmp", sizeof(double) * (size_t)kmax * m, &p)); tmp = (double*)p;
+  TRY(pool_get(c, "dc_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
+  TRY(pool_get(c, "dc_Qw", sizeof(double) * Nm, &p)); Qw = (double*)p;
+  TRY(pool_get(c, "dc_tau", sizeof(double) * m, &p)); tau = (double*)p;
+  TRY(pool_get(c, "dc_info", sizeof(int), &p)); info = (int*)p;
+  cudaStream_t st = c->stream;
+  const int32_t *d_is = (const int32_t*)c->d_is.ptr, *d_js = (const int32_t*)c->d_js.ptr,
+                *d_ks = (const int32_t*)c->d_ks.ptr, *d_ls = (const int32_t*)c->d_ls.ptr;
+  SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
+  const double one = 1.0, zero = 0.0;
+  std::vector<double> hE(m), hn(m);
+  int removed = 0, total = 0;
+  for (int pass = 0;; pass++) {
+    SS_CUDA_TRY(cudaMemsetAsync(tri, 0, sizeof(double) * T, st));
+    tri_fill_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, d_is, d_js, d_ks, d_ls, moy, tri);
+    // normalised Gaussian start vectors (src/davidson_clean.F90:137-149), orthonormalised
+    gaussian_matrix_kernel<<<m, 256, 0, st>>>(1, 0x44434c00u + (uint32_t)pass, N, m, U);
+    c->launches += 2;
+    TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+    TRY(op_apply(c, layout, N, m, tri, U, WU));
+    int k = m;
+    for (;;) {
+      if (++total > max_iter) {
+        ss_set_error_msg("davidson_clean: not converged after %d iterations (pass %d, residual %g)", max_iter,
+                         pass, hn[m / 2]);
+        return SS_ERR_NUMERIC;
+      }
+      // Rayleigh-Ritz on span(U): S = U^T H U, lowest m eigenpairs
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, k, N, &one, U, N, WU, N, &zero, S, k));
+      transpose_sym_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
+      c->launches++;
+      TRY(sym_eig(st, k, Sa, ev, ework, info, &c->launches));
+      ritz_cols_kernel<<<nb((int64_t)k * m), 256, 0, st>>>(k, m, Sa, tmp);
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, U, N, tmp, k, &zero, X, N));
+      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, WU, N, tmp, k, &zero, WX, N));
+      residual_kernel<<<nb((int64_t)N * m), 256, 0, st>>>(N, m, X, WX, ev, R);
+      col_norms_kernel<<<m, 256, 0, st>>>(N, m, R, nrm);
+      c->launches += 3;
+      int hinfo = 0;
+      SS_CUDA_TRY(cudaMemcpyAsync(hE.data(), ev, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hinfo) {
+        ss_set_error_msg("davidson_clean: projected eigenproblem did not converge");
+        return SS_ERR_NUMERIC;
+      }
+      double rmax = 0.0;
+      for (int j = 0; j < m; j++)
+        if (j <= m / 2 || hE[j] < -neg_eps) rmax = std::max(rmax, hn[j]);
+      if (rmax < tol || k == N) break;
+      if (k + m > kmax) {  // restart from the Ritz vectors (src/davidson_clean.F90:293-299)
+        SS_CUDA_TRY(cudaMemcpyAsync(U, X, sizeof(double) * Nm, cudaMemcpyDeviceToDevice, st));
+        TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+        TRY(op_apply(c, layout, N, m, tri, U, WU));
+        k = m;
+        continue;
+      }
+      double* Un = U + (size_t)k * N;
+      SS_CUDA_TRY(cudaMemcpyAsync(Un, R, sizeof(double) * Nm, cudaMemcpyDeviceToDevice, st));
+      TRY(orthonormalize_block(c, hb, N, k, m, U, Un, tmp, Qw, tau));
+      TRY(op_apply(c, layout, N, m, tri, Un, WU + (size_t)k * N));
+      k += m;
+    }
+    int nneg = 0;
+    while (nneg < m && hE[nneg] < -neg_eps) nneg++;  // ascending
+    if (nneg == 0) break;
+    deflate_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, d_is, d_js, d_ks, d_ls, nneg, ev, X, moy);
+    SS_CUDA_TRY(cudaGetLastError());
+    c->launches++;
+    removed += nneg;
+  }
+  SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));
+  SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (n_removed) *n_removed = removed;
+  return SS_OK;
+}
+
 }  // namespace ss
 
 using namespace ss;
@@ -648,6 +914,24 @@ int ss_davidson(ss_ctx* c, const double* moy, int layout, int m, double tol, int
     return SS_ERR_ARG;
   }
   return davidson(c, moy, layout, m, tol, max_iter, evals, evecs);
+}
+
+int ss_davidson_clean(ss_ctx* c, double* moy, int layout, int block, int max_blocks, double tol, int max_iter,
+                      int* n_removed) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  SS_CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->n || !c->nint) {
+    ss_set_error_msg("basis and quartets must be set first");
+    return SS_ERR_STATE;
+  }
+  if (!moy || (layout != SS_LAYOUT_REF_N2 && layout != SS_LAYOUT_PACKED_PAIR) || !(tol > 0.0) || max_iter < 1) {
+    ss_set_error_msg("ss_davidson_clean: bad arguments");
+    return SS_ERR_ARG;
+  }
+  return davidson_clean(c, moy, layout, block, max_blocks, tol, max_iter, n_removed);
 }
 
 }  // extern "C"
