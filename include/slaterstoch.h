@@ -138,6 +138,19 @@ int ss_job_result(ss_ctx* ctx, int64_t job_id, double* eri, double* sigma);
 /* Drop cached device results (Schwarz diagonal, analytic ERIs, MC sums); inputs stay. */
 int ss_invalidate(ss_ctx* ctx);
 
+/* Exact one-centre Slater ERIs (the do_exact_monocenter path, src/two_e_slater.F90:318-369,
+ * through compute_int_slater, src/compute_int_slater.F90): for every quartet of the list whose
+ * four functions share one centre (identical coordinates), out[q] = the exact ERI of the STOs
+ * themselves (src/ijkl_slater_xnynzn.F90) and mask[q] = 1; other quartets get 0 and 0.
+ * out/mask (nint) may be NULL; n_mono receives the number of one-centre quartets.
+ * SS_ERR_UNSUPPORTED if a one-centre quartet has a function beyond d (nx+ny+nz > 2), where the
+ * reference stops. */
+int ss_monocenter(ss_ctx* ctx, double* out, int32_t* mask, int64_t* n_mono);
+
+/* enable != 0: ss_combine, ss_two_e_job and the jobs give the one-centre quartets their exact
+ * value with MC mean and error bar 0 (src/two_e_slater.F90:465-494, 558-562). */
+int ss_set_exact_monocenter(ss_ctx* ctx, int enable);
+
 /* Largest MC error of the last ZV-MC run, and the number of blocks it used. */
 double ss_mc_max_sigma(const ss_ctx* ctx);
 int ss_mc_blocks_done(const ss_ctx* ctx);

@@ -63,6 +63,10 @@ def lib():
         L.orc_pair_densities.restype = None
         L.orc_pair_densities.argtypes = [C.POINTER(OrcBasis), C.c_int, i32p, i32p, C.c_int64,
                                          f64p, f64p, f64p]
+        L.orc_ijkl_slater_xnynzn.restype = C.c_int
+        L.orc_ijkl_slater_xnynzn.argtypes = [i32p, i32p, i32p, i32p, f64p, f64p]
+        L.orc_monocenter.restype = C.c_int64
+        L.orc_monocenter.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p, i32p, i32p, f64p, i32p]
         L.orc_one_elect.restype = None
         L.orc_one_elect.argtypes = [C.POINTER(OrcBasis), C.c_int, f64p, f64p, f64p, f64p, f64p]
         _lib = L
@@ -198,3 +202,26 @@ def one_elect(ob: OracleBasis, xyz, charge):
     S = np.zeros(n * n); V = np.zeros(n * n); K = np.zeros(n * n)
     lib().orc_one_elect(C.byref(ob.s), len(charge), xyz, charge, S, V, K)
     return (S.reshape(n, n, order="F"), V.reshape(n, n, order="F"), K.reshape(n, n, order="F"))
+
+
+def ijkl_slater_xnynzn(nix, niy, niz, power, gamma):
+    """Exact one-centre Slater ERI (1 2|3 4) of x^nx y^ny z^nz r^power e^(-gamma r) functions
+    (src/ijkl_slater_xnynzn.F90)."""
+    a = [np.ascontiguousarray(x, np.int32) for x in (nix, niy, niz, power)]
+    out = np.zeros(1)
+    rc = lib().orc_ijkl_slater_xnynzn(*a, np.ascontiguousarray(gamma, np.float64), out)
+    if rc:
+        raise ValueError("x^nx y^ny z^nz Slater functions beyond d are not implemented (as the reference)")
+    return float(out[0])
+
+
+def monocenter(ob: OracleBasis, quartets):
+    """Exact values of the one-centre quartets (src/two_e_slater.F90:318-369): (values, mask);
+    values are 0 where mask is 0."""
+    q = [np.ascontiguousarray(x, np.int32) for x in quartets]
+    out = np.zeros(len(q[0]))
+    mask = np.zeros(len(q[0]), np.int32)
+    cnt = lib().orc_monocenter(C.byref(ob.s), len(q[0]), *q, out, mask)
+    if cnt < 0:
+        raise ValueError("one-centre quartet with a function beyond d (not implemented, as the reference)")
+    return out, mask.astype(bool)

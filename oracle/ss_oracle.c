@@ -1253,3 +1253,218 @@ void orc_one_elect(const orc_basis *b, int nat, const double *xyz, const double 
       K[i + (int64_t)n * k] = kin;
     }
 }
+
+/* =====================================================================================
+ * Exact one-centre Slater ERIs: the do_exact_monocenter path (src/two_e_slater.F90:318-369)
+ * through compute_int_slater (src/compute_int_slater.F90:1-85), ijkl_slater_xnynzn
+ * (src/ijkl_slater_xnynzn.F90:1-158), ijkl_slater (src/ijkl_slater.F90:49-103), bigF
+ * (src/bigF.F90:1-34), smallg (src/smallg.F90:1-12), compute_lmin_lmax
+ * (src/compute_lmin_lmax.F90:1-25), norm_sto (src/norm_sto.F90:1-10).  The Gaunt coefficient
+ * (src/gaunt.F90, a third-party routine) is restated from its published definition: the
+ * Racah formula of the Wigner 3j symbol.
+ * ===================================================================================== */
+
+/* Wigner 3j symbol (j1 j2 j3; m1 m2 m3), Racah's single-sum formula */
+static double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0) return 0.0;
+  if (j3 < abs(j1 - j2) || j3 > j1 + j2) return 0.0;
+  if (abs(m1) > j1 || abs(m2) > j2 || abs(m3) > j3) return 0.0;
+  const double delta = fact(j1 + j2 - j3) * fact(j1 - j2 + j3) * fact(-j1 + j2 + j3) / fact(j1 + j2 + j3 + 1);
+  const double pre = sqrt(delta * fact(j1 + m1) * fact(j1 - m1) * fact(j2 + m2) * fact(j2 - m2) * fact(j3 + m3) *
+                          fact(j3 - m3));
+  int kmin = 0, kmax = j1 + j2 - j3;
+  if (j2 - j3 - m1 > kmin) kmin = j2 - j3 - m1;
+  if (j1 - j3 + m2 > kmin) kmin = j1 - j3 + m2;
+  if (j1 - m1 < kmax) kmax = j1 - m1;
+  if (j2 + m2 < kmax) kmax = j2 + m2;
+  double s = 0.0;
+  for (int k = kmin; k <= kmax; k++) {
+    const double t = 1.0 / (fact(k) * fact(j1 + j2 - j3 - k) * fact(j1 - m1 - k) * fact(j2 + m2 - k) *
+                            fact(j3 - j2 + m1 + k) * fact(j3 - j1 - m2 + k));
+    s += (k & 1) ? -t : t;
+  }
+  return (((j1 - j2 - m3) % 2 + 2) % 2 ? -1.0 : 1.0) * pre * s;
+}
+
+/* gaunt(l1,l2,l3,m1,m2,m3) = int dOmega Y*_{l1 m1} Y_{l2 m2} Y_{l3 m3}, m1 = m2 + m3
+ * (src/gaunt.F90:1-9, the calling convention of the reference) */
+static double gaunt(int l1, int l2, int l3, int m1, int m2, int m3) {
+  if (m1 - m2 - m3 != 0) return 0.0;
+  if ((l1 + l2 + l3) & 1) return 0.0;
+  const double c = sqrt((2.0 * l1 + 1.0) * (2.0 * l2 + 1.0) * (2.0 * l3 + 1.0) / (4.0 * acos(-1.0)));
+  return ((m1 % 2 + 2) % 2 ? -1.0 : 1.0) * c * wigner3j(l1, l2, l3, 0, 0, 0) * wigner3j(l1, l2, l3, -m1, m2, m3);
+}
+
+/* (src/norm_sto.F90:1-10) */
+static double norm_sto(double gam, int n) {
+  const double g = 2.0 * gam;
+  return sqrt(powi(g, 2 * n + 1) / fact(n + n));
+}
+
+/* (src/smallg.F90:1-12) */
+static double smallg(int n, int m, double g, double gp, int l) {
+  double s = 0.0;
+  for (int i = 0; i <= n + l; i++)
+    s = s + fact(n + l) * fact(n + m - 1 - i) / fact(n + l - i) / powi(g, i + 1) / powi(gp, n + m - i);
+  return s;
+}
+
+/* (src/bigF.F90:20-34) */
+static double bigF(int n12, double g12, int n34, double g34, int l) {
+  const int l12 = -l, l34 = l + 1;
+  const double g = g12 + g34;
+  const double first = fact(n34 + l34 - 1) / powi(g34, n34 + l34) * fact(n12 + l12 - 1) / powi(g12, n12 + l12);
+  return first + smallg(n34, n12, g34, g, l12 - 1) - smallg(n34, n12, g34, g, l34 - 1);
+}
+
+/* (src/compute_lmin_lmax.F90:1-25) */
+static void compute_lmin_lmax(int l1, int l2, int l3, int l4, int m1, int m2, int m3, int m4, int *lmin, int *lmax) {
+  *lmax = l1 + l2 < l3 + l4 ? l1 + l2 : l3 + l4;
+  const int mx12 = abs(l1 - l2) > abs(m1 - m2) ? abs(l1 - l2) : abs(m1 - m2);
+  const int l12min = ((*lmax + mx12) % 2 == 0) ? mx12 : mx12 + 1;
+  const int mx34 = abs(l3 - l4) > abs(m3 - m4) ? abs(l3 - l4) : abs(m3 - m4);
+  const int l34min = ((*lmax + mx34) % 2 == 0) ? mx34 : mx34 + 1;
+  *lmin = l12min > l34min ? l12min : l34min;
+}
+
+/* (src/ijkl_slater.F90:49-103) */
+static double ijkl_slater(const int *nslat, const int *lslat, const int *mslat, const double *gamma) {
+  const int l1 = lslat[0], l2 = lslat[1], l3 = lslat[2], l4 = lslat[3];
+  if ((l1 + l2 + l3 + l4) % 2 == 1) return 0.0;
+  const int m1 = mslat[0], m2 = mslat[1], m3 = mslat[2], m4 = mslat[3];
+  if (m2 - m1 != m3 - m4) return 0.0;
+  const int m = m2 - m1;
+  const double pi = acos(-1.0);
+  double norm = 1.0;
+  for (int i = 0; i < 4; i++) norm = norm * norm_sto(gamma[i], nslat[i]);
+  int lmin, lmax;
+  compute_lmin_lmax(l1, l2, l3, l4, m1, m2, m3, m4, &lmin, &lmax);
+  const int n12 = nslat[0] + nslat[1], n34 = nslat[2] + nslat[3];
+  const double g12 = gamma[0] + gamma[1], g34 = gamma[2] + gamma[3];
+  double s = 0.0;
+  for (int l = lmin; l <= lmax; l += 2)
+    s = s + gaunt(l2, l, l1, m2, m, m1) * gaunt(l3, l, l4, m3, m, m4) * bigF(n12, g12, n34, g34, l) / (2.0 * l + 1.0);
+  return 4.0 * pi * s * norm;
+}
+
+/* complex coefficients of x^nx y^ny z^nz / r^(nx+ny+nz) over Y_l^m, nx+ny+nz <= 2
+ * (src/ijkl_slater_xnynzn.F90:59-124) */
+static void xyz_ylm_coef(double re[3][3][3][3][5], double im[3][3][3][3][5]) {
+  memset(re, 0, sizeof(double) * 3 * 3 * 3 * 3 * 5);
+  memset(im, 0, sizeof(double) * 3 * 3 * 3 * 3 * 5);
+  const double pi = acos(-1.0);
+  const double r4 = sqrt(4.0 * pi), r43 = sqrt(4.0 * pi / 3.0), r15 = sqrt(pi / 15.0), s2 = sqrt(2.0),
+               s3 = sqrt(3.0);
+#define C(nx, ny, nz, l, m) [nx][ny][nz][l][(m) + 2]
+  re C(0, 0, 0, 0, 0) = r4;
+  re C(1, 0, 0, 1, -1) = r43 / s2;
+  re C(1, 0, 0, 1, 1) = -r43 / s2;
+  im C(0, 1, 0, 1, -1) = r43 / s2;
+  im C(0, 1, 0, 1, 1) = r43 / s2;
+  re C(0, 0, 1, 1, 0) = r43;
+  im C(1, 1, 0, 2, -2) = r15 * s2;
+  im C(1, 1, 0, 2, 2) = -r15 * s2;
+  im C(0, 1, 1, 2, -1) = r15 * s2;
+  im C(0, 1, 1, 2, 1) = r15 * s2;
+  re C(1, 0, 1, 2, -1) = r15 * s2;
+  re C(1, 0, 1, 2, 1) = -r15 * s2;
+  re C(2, 0, 0, 0, 0) = r4 / 3.0;
+  re C(2, 0, 0, 2, -2) = r15 * s2;
+  re C(2, 0, 0, 2, 2) = r15 * s2;
+  re C(2, 0, 0, 2, 0) = -r15 * 2.0 / s3;
+  re C(0, 2, 0, 0, 0) = r4 / 3.0;
+  re C(0, 2, 0, 2, -2) = -r15 * s2;
+  re C(0, 2, 0, 2, 2) = -r15 * s2;
+  re C(0, 2, 0, 2, 0) = -r15 * 2.0 / s3;
+  re C(0, 0, 2, 0, 0) = r4 / 3.0;
+  re C(0, 0, 2, 2, 0) = r15 * 4.0 / s3;
+#undef C
+}
+
+/* (src/ijkl_slater_xnynzn.F90:1-158); returns -1 for a function with nx+ny+nz > 2 (the
+ * reference stops there) */
+int orc_ijkl_slater_xnynzn(const int *nix, const int *niy, const int *niz, const int *power, const double *gamma,
+                           double *out) {
+  static double cre[3][3][3][3][5], cim[3][3][3][3][5];
+  static int have = 0;
+  if (!g_init) init_tables();
+  for (int k = 0; k < 4; k++)
+    if (nix[k] + niy[k] + niz[k] > 2) return -1;
+  if (!have) {
+#ifdef _OPENMP
+#pragma omp critical(orc_xyz_ylm)
+#endif
+    {
+      if (!have) {
+        xyz_ylm_coef(cre, cim);
+        have = 1;
+      }
+    }
+  }
+  int nslat[4], lmax[4];
+  for (int k = 0; k < 4; k++) {
+    nslat[k] = 1 + nix[k] + niy[k] + niz[k] + power[k];
+    lmax[k] = nix[k] + niy[k] + niz[k];
+  }
+  double rre = 0.0, rim = 0.0;
+  for (int l1 = 0; l1 <= lmax[0]; l1++)
+    for (int m1 = -l1; m1 <= l1; m1++)
+      for (int l2 = 0; l2 <= lmax[1]; l2++)
+        for (int m2 = -l2; m2 <= l2; m2++)
+          for (int l3 = 0; l3 <= lmax[2]; l3++)
+            for (int m3 = -l3; m3 <= l3; m3++)
+              for (int l4 = 0; l4 <= lmax[3]; l4++)
+                for (int m4 = -l4; m4 <= l4; m4++) {
+                  const int ls[4] = {l1, l2, l3, l4};
+                  const int ms[4] = {-m1, m2, -m3, m4};
+                  const int lm[4][2] = {{l1, m1}, {l2, m2}, {l3, m3}, {l4, m4}};
+                  double cr = 1.0, ci = 0.0;
+                  for (int t = 0; t < 4; t++) {
+                    const double ar = cre[nix[t]][niy[t]][niz[t]][lm[t][0]][lm[t][1] + 2];
+                    const double ai = cim[nix[t]][niy[t]][niz[t]][lm[t][0]][lm[t][1] + 2];
+                    const double nr = cr * ar - ci * ai, ni = cr * ai + ci * ar;
+                    cr = nr;
+                    ci = ni;
+                  }
+                  if (sqrt(cr * cr + ci * ci) > 1.e-20) {
+                    const double v = (((m1 + m3) % 2 + 2) % 2 ? -1.0 : 1.0) * ijkl_slater(nslat, ls, ms, gamma);
+                    rre = rre + cr * v;
+                    rim = rim + ci * v;
+                  }
+                }
+  double norm = 1.0;
+  for (int k = 0; k < 4; k++) norm = norm * norm_sto(gamma[k], nslat[k]);
+  *out = rre / norm;
+  return 0;
+}
+
+/* One-centre quartets of the list (all four functions on one centre, src/two_e_slater.F90:
+ * 318-327) get compute_int_slater(i,k,j,l) (src/compute_int_slater.F90); mask[q] = 1 for
+ * them, 0 (and out[q] untouched) for the others.  Returns the number of one-centre quartets,
+ * or -1 if one of them has a function with nx+ny+nz > 2. */
+int64_t orc_monocenter(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js, const int32_t *ks,
+                       const int32_t *ls, double *out, int32_t *mask) {
+  int64_t count = 0;
+  int bad = 0;
+  for (int64_t q = 0; q < nint; q++) {
+    const int f[4] = {is[q] - 1, ks[q] - 1, js[q] - 1, ls[q] - 1}; /* (i, k, j, l) */
+    int same = 1;
+    for (int t = 1; t < 4; t++)
+      for (int a = 0; a < 3; a++)
+        if (b->center[3 * f[t] + a] != b->center[3 * f[0] + a]) same = 0;
+    mask[q] = same;
+    if (!same) continue;
+    int nx[4], ny[4], nz[4], pw[4];
+    double gam[4];
+    for (int t = 0; t < 4; t++) {
+      nx[t] = b->npower[3 * f[t]];
+      ny[t] = b->npower[3 * f[t] + 1];
+      nz[t] = b->npower[3 * f[t] + 2];
+      pw[t] = b->n_sto[f[t]];
+      gam[t] = b->g_slater[f[t]];
+    }
+    if (orc_ijkl_slater_xnynzn(nx, ny, nz, pw, gam, &out[q])) bad = 1;
+    count++;
+  }
+  return bad ? -1 : count;
+}

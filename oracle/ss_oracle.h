@@ -105,6 +105,16 @@ void orc_pair_densities(const orc_basis *b, int npairs, const int *ip, const int
  * one_electron_sij.F90, one_electron_Kij.F90, one_electron_Vij.F90, NAI_pol_mult.F90):
  * overlap S, nuclear attraction V (nuclei xyz[3*nat] bohr, charge[nat]) and kinetic K,
  * column-major n x n (X[i + n*k]). */
+/* Exact one-centre Slater ERI of x^nix y^niy z^niz r^power e^(-gamma r) functions in the
+ * order (1 2 | 3 4) (src/ijkl_slater_xnynzn.F90); -1 if a function has nix+niy+niz > 2. */
+int orc_ijkl_slater_xnynzn(const int *nix, const int *niy, const int *niz, const int *power,
+                           const double *gamma, double *out);
+
+/* Exact values of the one-centre quartets of the list (src/two_e_slater.F90:318-369); mask[q]
+ * = 1 for them.  Returns their number, -1 if one has a function beyond d. */
+int64_t orc_monocenter(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                       const int32_t *ks, const int32_t *ls, double *out, int32_t *mask);
+
 void orc_one_elect(const orc_basis *b, int nat, const double *xyz, const double *charge, double *S, double *V,
                    double *K);
 

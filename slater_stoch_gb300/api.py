@@ -152,6 +152,20 @@ class Context:
         _lib.check(self._L.ss_one_e(self._h, _ptr(S), _ptr(V), _ptr(K)))
         return S.reshape(n, n, order="F"), V.reshape(n, n, order="F"), K.reshape(n, n, order="F")
 
+    # -- exact one-centre integrals -------------------------------------------------
+    def monocenter(self):
+        """Exact one-centre Slater ERIs of the quartet list: (values, mask); values are 0
+        where mask is False (src/compute_int_slater.F90)."""
+        out = np.zeros(self.nint)
+        mask = np.zeros(self.nint, np.int32)
+        cnt = np.zeros(1, np.int64)
+        _lib.check(self._L.ss_monocenter(self._h, _ptr(out), _ptr(mask), _ptr(cnt)))
+        return out, mask.astype(bool)
+
+    def set_exact_monocenter(self, enable: bool = True):
+        """One-centre quartets take their exact value (MC error 0) in combine/two_e_job/jobs."""
+        _lib.check(self._L.ss_set_exact_monocenter(self._h, int(bool(enable))))
+
     # -- output ----------------------------------------------------------------------
     def write_bielec_ao(self, path):
         """The reference's bielec_ao text file of the last job's merged ERIs and MC errors."""

@@ -12,6 +12,9 @@
 
 namespace ss {
 
+int ensure_mono(ss_ctx* c);
+int launch_combine_mono(ss_ctx* c, double* out);
+
 __global__ void combine_kernel(int64_t nint, const double* __restrict__ g, const double* __restrict__ m,
                                double* __restrict__ out) {
   int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -296,7 +299,7 @@ int ss_invalidate(ss_ctx* c) {
     ss_set_error_msg("null ss_ctx");
     return SS_ERR_ARG;
   }
-  c->have_precond = c->have_gauss = c->have_mc = false;
+  c->have_precond = c->have_gauss = c->have_mc = c->have_mono = false;
   return SS_OK;
 }
 
@@ -324,10 +327,15 @@ int ss_combine(ss_ctx* c, double* out) {
   TRY(ensure_gauss(c));
   void* o;
   TRY(pool_get(c, "combined", sizeof(double) * c->nint, &o));
-  combine_kernel<<<(unsigned)((c->nint + 255) / 256), 256, 0, c->stream>>>(
-      c->nint, (const double*)c->d_gauss.ptr, (const double*)c->d_mean.ptr, (double*)o);
-  SS_CUDA_TRY(cudaGetLastError());
-  c->launches++;
+  if (c->exact_monocenter) {  // src/two_e_slater.F90:558-564 with do_exact_monocenter
+    TRY(ensure_mono(c));
+    TRY(launch_combine_mono(c, (double*)o));
+  } else {
+    combine_kernel<<<(unsigned)((c->nint + 255) / 256), 256, 0, c->stream>>>(
+        c->nint, (const double*)c->d_gauss.ptr, (const double*)c->d_mean.ptr, (double*)o);
+    SS_CUDA_TRY(cudaGetLastError());
+    c->launches++;
+  }
   if (out) SS_CUDA_TRY(cudaMemcpyAsync(out, o, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, c->stream));
   SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return SS_OK;

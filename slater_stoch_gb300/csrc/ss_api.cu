@@ -400,7 +400,8 @@ void ss_destroy(ss_ctx* c) {
   DevBuf* bufs[] = {&c->d_center, &c->d_npower, &c->d_nsto, &c->d_itype, &c->d_ng, &c->d_cg, &c->d_gg,
                     &c->d_gs, &c->d_pp, &c->d_ppf, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
                     &c->d_ls, &c->d_precond, &c->d_gauss, &c->d_mean, &c->d_sigma, &c->d_scratch_a,
-                    &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d};
+                    &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d, &c->d_mono_val, &c->d_mono_mask,
+                    &c->d_mono_status};
   for (DevBuf* b : bufs) dev_free(c, *b);
   for (auto& kv : c->pool) dev_free(c, kv.second);
   destroy_cublas(c->cublas_handle);
@@ -496,7 +497,7 @@ int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower,
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;
   c->have_precond = c->have_gauss = c->have_mc = false;
-  c->have_resid = false;
+  c->have_resid = c->have_mono = false;
   return SS_OK;
 }
 
@@ -532,7 +533,7 @@ int ss_quartets_set(ss_ctx* c, int64_t nint, const int32_t* is, const int32_t* j
   rc |= h2d(c, c->d_ls, ls, sizeof(int32_t) * nint);
   (void)b;
   if (rc) return SS_ERR_NOMEM;
-  c->have_gauss = c->have_mc = false;
+  c->have_gauss = c->have_mc = c->have_mono = false;
   return SS_OK;
 }
 

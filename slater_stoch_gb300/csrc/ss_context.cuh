@@ -77,6 +77,12 @@ struct ss_ctx {
   ss::DevBuf d_precond, d_gauss;
   int64_t n_removed = 0;
 
+  // exact one-centre Slater ERIs (monocenter.cu)
+  bool exact_monocenter = false;  // ss_set_exact_monocenter: used by ss_combine and the jobs
+  bool have_mono = false;
+  int64_t n_mono = 0;
+  ss::DevBuf d_mono_val, d_mono_mask, d_mono_status;
+
   // MC results
   bool have_mc = false;
   bool have_resid = false;  // shared-walker residual tables of the current basis (pool "rs_*")
