@@ -138,9 +138,11 @@ def test_davidson_clean_matches_exact_projection(cfg, block, blocks):
         got, nrem = ctx.davidson_clean(moy, layout="packed_pair", block=block, max_blocks=blocks, tol=1e-8)
     ref, nref = OC.psd_project(moy, q, b.n, "packed_pair")
     scale = np.abs(moy).max()
-    assert nrem == nref and nrem > 0
-    assert np.max(np.abs(got - ref)) <= 1e-11 * scale
-    assert np.linalg.eigvalsh(OC.matrix_from_eris(got, q, b.n, "packed_pair")).min() >= -1e-11
+    diff = np.max(np.abs(got - ref)) / scale
+    lmin = np.linalg.eigvalsh(OC.matrix_from_eris(got, q, b.n, "packed_pair")).min()
+    # a converged Ritz pair (residual < tol) leaves a rounding-level remainder that a later
+    # search may deflate as well, so the count can exceed the exact projection's
+    assert nrem >= nref > 0 and diff <= 1e-11 and lmin >= -1e-11, (nrem, nref, diff, lmin)
 
 
 def test_davidson_clean_restarted_basis():
