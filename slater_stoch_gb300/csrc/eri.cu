@@ -30,6 +30,25 @@ namespace ss {
 
 constexpr double THRESH = 1.e-15;
 
+// Functions i and k on the same centre with the same fit (exponents, coefficients, fit type)
+// give bit-identical primitive-pair records for (m1, m2) and (m2, m1): the same Gaussian
+// product (a A + b A = b A + a A), centre offsets and coefficient product, and the polynomial
+// (x - A)^(a_i + a_k) does not depend on which exponent goes with which function.  This holds
+// for i = k and for the cartesian components of one shell (px/py/pz, the six d's).
+__device__ bool fold_pair(const BasisDev& B, int i, int k) {
+  if (i == k) return true;
+  const int ng = B.n_gauss[i];
+  if (ng != B.n_gauss[k] || B.i_type[i] != B.i_type[k]) return false;
+  for (int ax = 0; ax < 3; ax++)
+    if (B.center[3 * i + ax] != B.center[3 * k + ax]) return false;
+  const int64_t t = B.i_type[i] == 2 ? 1 : 0;
+  for (int m = 0; m < ng; m++) {
+    if (B.g_gauss[m + (int64_t)B.ld * i] != B.g_gauss[m + (int64_t)B.ld * k]) return false;
+    if (B.c_gauss[m + (int64_t)B.ld * (i + B.n * t)] != B.c_gauss[m + (int64_t)B.ld * (k + B.n * t)]) return false;
+  }
+  return true;
+}
+
 __global__ void prim_pair_count(BasisDev B, int npairs, int* __restrict__ cnt) {
   int pidx = blockIdx.x;
   if (pidx >= npairs) return;
@@ -43,10 +62,11 @@ __global__ void prim_pair_count(BasisDev B, int npairs, int* __restrict__ cnt) {
   const int ngi = B.n_gauss[i], ngk = B.n_gauss[k];
   const double* A = B.center + 3 * i;
   const double* Bc = B.center + 3 * k;
+  const bool fold = fold_pair(B, i, k);
   int local = 0;
   for (int t = threadIdx.x; t < ngi * ngk; t += blockDim.x) {
     int m1 = t / ngk, m2 = t % ngk;
-    if (i == k && m2 < m1) continue;  // folded into (m2, m1), see prim_pair_fill
+    if (fold && m2 < m1) continue;  // folded into (m2, m1), see prim_pair_fill
     double a = B.g_gauss[m1 + (int64_t)B.ld * i], b = B.g_gauss[m2 + (int64_t)B.ld * k];
     double p_inv = 1.0 / (a + b);
     double ab = a * b;
@@ -75,13 +95,13 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
   const double* Bc = B.center + 3 * k;
   const int ti = B.i_type[i] == 2 ? 1 : 0, tk = B.i_type[k] == 2 ? 1 : 0;
   // sequential compaction in (m1, m2) order by thread 0 (ng <= 30: at most 900 entries).
-  // A diagonal function pair (i = k) gives identical Gaussian products, centres, polynomials and
-  // coefficient products for (m1, m2) and (m2, m1): only m1 <= m2 is kept, with the coefficient
-  // doubled for m1 < m2 (exact), which halves the primitive pairs of those functions.
+  // For a folded pair (fold_pair) only m1 <= m2 is kept, with the coefficient doubled for
+  // m1 < m2 (exact), which halves the primitive pairs of those function pairs.
   if (threadIdx.x != 0) return;
+  const bool fold = fold_pair(B, i, k);
   int64_t o = off[pidx];
   for (int m1 = 0; m1 < ngi; m1++)
-    for (int m2 = (i == k ? m1 : 0); m2 < ngk; m2++) {
+    for (int m2 = (fold ? m1 : 0); m2 < ngk; m2++) {
       double a = B.g_gauss[m1 + (int64_t)B.ld * i], b = B.g_gauss[m2 + (int64_t)B.ld * k];
       // src/gaussian_product.F90:17-32
       double p = a + b;
@@ -105,7 +125,7 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
       }
       r.coef = B.c_gauss[m1 + (int64_t)B.ld * (i + (int64_t)B.n * ti)] *
                B.c_gauss[m2 + (int64_t)B.ld * (k + (int64_t)B.n * tk)];
-      if (i == k && m1 != m2) r.coef = 2.0 * r.coef;
+      if (fold && m1 != m2) r.coef = 2.0 * r.coef;
       r.pad[0] = 0.0;                    // Schwarz factor, set by the ERI kernel's self mode
       r.pad[1] = (double)(m1 * ngk + m2);  // position in the reference's (m1, m2) loop
       r.pad[2] = 0.0;
