@@ -529,6 +529,10 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
   const int b0 = part * per;
   const int b1 = min(nb, b0 + per);
   const int nbs = max(b1 - b0, 0);
+  if (nbs == 0) {  // an empty bra slice (more slices than bra pairs): block-uniform exit
+    if (threadIdx.x == 0) partial[w * split + part] = 0.0;
+    return;
+  }
   double acc = 0.0;
   float acc32 = 0.f;
 

@@ -115,11 +115,6 @@ static int pair_L(const ss_ctx* c, int f1, int f2) {
   return L;
 }
 
-static int total_pow(const ss_ctx* c, int f) {
-  return c->h_npower[3 * f] + c->h_npower[3 * f + 1] + c->h_npower[3 * f + 2] +
-         (c->h_itype[f] == 2 ? 2 : 0);
-}
-
 // Run the ERI kernels for the quartets listed in (qis..qls) restricted to `sel` (indices into
 // them); partial sums are written to d_scratch_b and slot[q] gives the partial row of q.
 static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const int32_t* d_qks,
@@ -137,7 +132,8 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     bucket[5 * L + nt].push_back(t);
   }
   // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes
-  // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 64 ways).
+  // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 127 ways,
+  // the largest split a slot code holds).
   const int64_t target = (int64_t)c->num_sms * 8;
   std::vector<int64_t> work;
   work.reserve(sel.size());
@@ -147,7 +143,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   for (int bk = 0; bk < NB; bk++) {
     begin[bk] = (int64_t)work.size();
     const int64_t cnt = (int64_t)bucket[bk].size();
-    bsplit[bk] = cnt ? (int)std::min<int64_t>(64, std::max<int64_t>(1, (target + cnt - 1) / cnt)) : 1;
+    bsplit[bk] = cnt ? (int)std::min<int64_t>((1 << SLOT_SPLIT_BITS) - 1,
+                                              std::max<int64_t>(1, (target + cnt - 1) / cnt))
+                     : 1;
     int64_t local = 0;
     for (int64_t t : bucket[bk]) {
       slot_of_sel[t] = ((pbase[bk] + local * bsplit[bk]) << SLOT_SPLIT_BITS) | bsplit[bk];
@@ -167,8 +165,26 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   if (rc) return rc;
   const int64_t* d_work = (const int64_t*)c->d_scratch_a.ptr;
   double* d_partial = (double*)c->d_scratch_b.ptr;
-  for (int bk = 0; bk < NB; bk++) {
-    if (!count[bk]) continue;
+  // classes launched round-robin over the side streams, largest launch first; the side streams
+  // start after everything queued on the context stream and the context stream waits for all
+  if (!c->eri_fork) {
+    for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
+      SS_CUDA_TRY(cudaStreamCreateWithFlags(&c->eri_stream[s], cudaStreamNonBlocking));
+      SS_CUDA_TRY(cudaEventCreateWithFlags(&c->eri_join[s], cudaEventDisableTiming));
+    }
+    SS_CUDA_TRY(cudaEventCreateWithFlags(&c->eri_fork, cudaEventDisableTiming));
+  }
+  std::vector<int> order;
+  for (int bk = 0; bk < NB; bk++)
+    if (count[bk]) order.push_back(bk);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return count[a] * bsplit[a] > count[b] * bsplit[b]; });
+  SS_CUDA_TRY(cudaEventRecord(c->eri_fork, c->stream));
+  for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) SS_CUDA_TRY(cudaStreamWaitEvent(c->eri_stream[s], c->eri_fork, 0));
+  int launch_rc = SS_OK;
+  for (size_t oi = 0; oi < order.size() && !launch_rc; oi++) {
+    const int bk = order[oi];
+    cudaStream_t st = c->eri_stream[oi % ss_ctx::ERI_STREAMS];
     const int L = bk / 5;
     const int tc = bk % 5;
     const bool t2 = tc > 0;
@@ -181,19 +197,24 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     for (int64_t s0 = 0; s0 < count[bk]; s0 += chunk) {
       int64_t nq = std::min(chunk, count[bk] - s0);
       dim3 grid((unsigned)(nq * split));
-      cudaError_t e = launch_eri_class(L, tc, grid, ktile, smem, c->stream, c->basis,
+      cudaError_t e = launch_eri_class(L, tc, grid, ktile, smem, st, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
                                        d_qjs, d_qks, d_qls, d_pre, eps, d_partial + pbase[bk] + s0 * split,
                                        self_out, (const PrimPairF*)c->d_ppf.ptr);
       if (e != cudaSuccess) {
         ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
-        return SS_ERR_CUDA;
+        launch_rc = SS_ERR_CUDA;
+        break;
       }
       c->launches++;
     }
   }
-  return SS_OK;
+  for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
+    SS_CUDA_TRY(cudaEventRecord(c->eri_join[s], c->eri_stream[s]));
+    SS_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->eri_join[s], 0));
+  }
+  return launch_rc;
 }
 
 int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out) {
@@ -405,6 +426,11 @@ void ss_destroy(ss_ctx* c) {
   for (DevBuf* b : bufs) dev_free(c, *b);
   for (auto& kv : c->pool) dev_free(c, kv.second);
   destroy_cublas(c->cublas_handle);
+  for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
+    if (c->eri_stream[s]) cudaStreamDestroy(c->eri_stream[s]);
+    if (c->eri_join[s]) cudaEventDestroy(c->eri_join[s]);
+  }
+  if (c->eri_fork) cudaEventDestroy(c->eri_fork);
   cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -47,6 +47,11 @@ struct ss_ctx {
   int device = 0;
   size_t budget = 0, used = 0;
   cudaStream_t stream = nullptr;
+  // side streams of the analytic stage: the ERI classes are launched across them so that one
+  // class's CTAs fill the tail of another's launch (created on first use)
+  static constexpr int ERI_STREAMS = 4;
+  cudaStream_t eri_stream[ERI_STREAMS] = {};
+  cudaEvent_t eri_fork = nullptr, eri_join[ERI_STREAMS] = {};
   int64_t launches = 0;
   int num_sms = 0;
 
