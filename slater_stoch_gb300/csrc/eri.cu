@@ -160,11 +160,12 @@ __global__ void eri_finalize(int64_t nint, const int32_t* __restrict__ is, const
 cudaError_t eri_init_constants() { return cudaSuccess; }  // tables are compile-time
 
 // ket pairs per shared-memory tile and the dynamic shared memory it needs
-void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem) {
+void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem) {
   const int no = t2 ? 4 : 1;
-  // per ket pair: the record and its polynomials in FP64, and their FP32 copies
-  const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (L + 1) + 6 * sizeof(float) +
-                     sizeof(float) * 3 * no * (L + 1);
+  // per ket pair: the record and its polynomials (ket degree bound LK) in FP64, and their FP32
+  // copies
+  const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (LK + 1) + 6 * sizeof(float) +
+                     sizeof(float) * 3 * no * (LK + 1);
   // Small ket tiles: with ~53 KB of static tables and scans, 60 KB tiles let two CTAs share an
   // SM (8 warps) and leave unified L1 to the local arrays of the classes with r^2-type fits.  On
   // the 26-function H2O basis 168 KB (one CTA per SM) -> 60 KB tiles took the analytic stage from
@@ -190,15 +191,32 @@ cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, co
 cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c4(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 
-// Kernel instance for class (L, tc).  tc: number of r^2-type fits among the four functions
-// (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has L = 4; an
-// instance with a larger L serves any smaller one (degrees are runtime).
-cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
+// Kernel instance for class (L, tc) and ket bound LK.  tc: number of r^2-type fits among the
+// four functions (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has
+// L = 4; an instance with a larger L serves any smaller one (degrees are runtime).  LK = 1 < L
+// (L = 3, 4; its r^2-type fits, at most two, all in the bra): the light-ket instances.
+cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
                              double* partial, double* self_out, const PrimPairF* ppf) {
+  if (LK < L) {
+    if (LK != 1 || L < 3 || tc > 2) return cudaErrorInvalidValue;
+#define SS_K1(LL, TT)                                                                                          \
+  if (L == LL && tc == TT)                                                                                     \
+    return launch_eri_L##LL##c##TT##k1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, \
+                                       eps, partial, self_out, ppf);
+    SS_K1(3, 0) SS_K1(3, 1) SS_K1(3, 2) SS_K1(4, 0) SS_K1(4, 1) SS_K1(4, 2)
+#undef SS_K1
+    return cudaErrorInvalidValue;
+  }
   if (tc == 0) {
     if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
     if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);

@@ -82,17 +82,17 @@ struct RecCoefT {
   Real p10_1, p10_2, p01_1, p01_2, pq_inv;
 };
 
-// Bottom-up table I(a,c)[m] (coefficients of u = t^2) for a <= amax, c <= cmax (both <= L),
+// Bottom-up table I(a,c)[m] (coefficients of u = t^2) for a <= amax <= L, c <= cmax <= LK,
 // the same per-coefficient operation order as I_x1_pol_mult / I_x2_pol_mult:
 //   I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1);  I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
-template <int L, typename Real>
+template <int L, int LK, typename Real>
 __device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int cmax,
-                                          Real (&I)[L + 1][L + 1][2 * L + 1]) {
+                                          Real (&I)[L + 1][LK + 1][L + LK + 1]) {
 #pragma unroll
-  for (int c = 0; c <= L; c++) {
+  for (int c = 0; c <= LK; c++) {
     if (c > cmax) break;
 #pragma unroll
-    for (int m = 0; m <= 2 * L; m++) {
+    for (int m = 0; m <= LK; m++) {
       if (m > c) break;
       Real v = Real(0);
       if (c == 0) {
@@ -111,10 +111,10 @@ __device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real
   for (int a = 1; a <= L; a++) {
     if (a > amax) break;
 #pragma unroll
-    for (int c = 0; c <= L; c++) {
+    for (int c = 0; c <= LK; c++) {
       if (c > cmax) break;
 #pragma unroll
-      for (int m = 0; m <= 2 * L; m++) {
+      for (int m = 0; m <= L + LK; m++) {
         if (m > a + c) break;
         Real v = Real(0);
         if (a >= 2) {
@@ -132,14 +132,14 @@ __device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real
 
 // The same table when bra and ket share one centre (all four functions on one atom): C00 and
 // D00 vanish, so only the B10/B01/B00 terms remain and every entry with a + c odd is zero.
-template <int L, typename Real>
+template <int L, int LK, typename Real>
 __device__ __forceinline__ void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
-                                             Real (&I)[L + 1][L + 1][2 * L + 1]) {
+                                             Real (&I)[L + 1][LK + 1][L + LK + 1]) {
 #pragma unroll
-  for (int c = 0; c <= L; c++) {
+  for (int c = 0; c <= LK; c++) {
     if (c > cmax) break;
 #pragma unroll
-    for (int m = 0; m <= 2 * L; m++) {
+    for (int m = 0; m <= LK; m++) {
       if (m > c) break;
       Real v = Real(0);
       if (c == 0) {
@@ -155,10 +155,10 @@ __device__ __forceinline__ void rys_table_1c(const RecCoefT<Real>& R, int amax, 
   for (int a = 1; a <= L; a++) {
     if (a > amax) break;
 #pragma unroll
-    for (int c = 0; c <= L; c++) {
+    for (int c = 0; c <= LK; c++) {
       if (c > cmax) break;
 #pragma unroll
-      for (int m = 0; m <= 2 * L; m++) {
+      for (int m = 0; m <= L + LK; m++) {
         if (m > a + c) break;
         Real v = Real(0);
         if (!((a + c) & 1)) {
@@ -187,24 +187,24 @@ __device__ __forceinline__ bool abs_gt(float x, float t) { return (__float_as_in
 
 // Ix = sum_{ix,jx} (Pn[ix] Qn[jx]) I(ix,jx) with the thresholds of general_primitive_integral
 // (x axis: skip |P| < thresh; y, z: keep |P| > thresh; skip |P Q| < thresh).
-template <int L, typename Real>
+template <int L, int LK, typename Real>
 __device__ __forceinline__ void axis_poly(const Real* Pn, int degP, const Real* Qn, int degQ,
-                                          const Real (&I)[L + 1][L + 1][2 * L + 1], bool x_axis,
+                                          const Real (&I)[L + 1][LK + 1][L + LK + 1], bool x_axis,
                                           Real* out) {
 #pragma unroll
-  for (int m = 0; m <= 2 * L; m++) out[m] = Real(0);
+  for (int m = 0; m <= L + LK; m++) out[m] = Real(0);
 #pragma unroll
   for (int ix = 0; ix <= L; ix++) {
     if (ix > degP) break;
     const Real a = Pn[ix];
     if (x_axis ? abs_lt(a, (Real)THRESH) : !abs_gt(a, (Real)THRESH)) continue;
 #pragma unroll
-    for (int jx = 0; jx <= L; jx++) {
+    for (int jx = 0; jx <= LK; jx++) {
       if (jx > degQ) break;
       const Real d = a * Qn[jx];
       if (abs_lt(d, (Real)THRESH)) continue;
 #pragma unroll
-      for (int m = 0; m <= 2 * L; m++)
+      for (int m = 0; m <= L + LK; m++)
         if (m <= ix + jx) out[m] = fma(d, I[ix][jx][m], out[m]);
     }
   }
@@ -306,13 +306,15 @@ __device__ __forceinline__ PairView<float> view32(const PrimPairF& A) {
 // components of the r^2-type fits): returns pref * sum_n d1[n] F_n; the caller multiplies by
 // the coefficient product P.coef * Q.coef.  Pn, Qn: pair_polys of the bra and ket pairs.
 // TC: the number of r^2-type fits among the four functions (0..4; with any, the subset recursion
-// over the axes below).
-template <int L, int TC, typename Real>
+// over the axes below).  L bounds the per-axis degree of the bra pair, LK that of the ket pair
+// (Pn: [ax][o][L+1], Qn: [ax][o][LK+1]); the total degree is at most 3 (L + LK).
+template <int L, int TC, typename Real, int LK = L>
 __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const Real* Pn,
                                              const PairView<Real>& Q, const Real* Qn, const Real* s_boys) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;
-  constexpr int NF = (6 * L < 16) ? 6 * L : 16;
+  constexpr int LT = L + LK;                       // per-axis degree bound of the quartet
+  constexpr int NF = (3 * LT < 16) ? 3 * LT : 16;
   const Real p = P.p, qq = Q.p;
   // src/general_primitive_integral.F90:54-60, 142-146
   const Real pq = P.p_inv * Real(0.5) * Q.p_inv;
@@ -337,7 +339,7 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
 
   Real accu;
   if (!T2) {
-    Real A[3][2 * L + 1];
+    Real A[3][LT + 1];
     int deg[3];
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
@@ -345,25 +347,25 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
       if (deg[ax] == 0) {
         A[ax][0] = Real(1);
 #pragma unroll
-        for (int m = 1; m <= 2 * L; m++) A[ax][m] = Real(0);
+        for (int m = 1; m <= LT; m++) A[ax][m] = Real(0);
         continue;
       }
-      Real I[L + 1][L + 1][2 * L + 1];
+      Real I[L + 1][LK + 1][LT + 1];
       const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
       const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
-      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
-      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
-      axis_poly<L>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (L + 1), S.cmax[ax], I, ax == 0, A[ax]);
+      if (S.onec) rys_table_1c<L, LK>(R, S.amax[ax], S.cmax[ax], I);
+      else rys_table<L, LK>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      axis_poly<L, LK>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (LK + 1), S.cmax[ax], I, ax == 0, A[ax]);
     }
     // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
-    Real dp[4 * L + 1];
+    Real dp[2 * LT + 1];
 #pragma unroll
-    for (int t = 0; t <= 4 * L; t++) dp[t] = Real(0);
+    for (int t = 0; t <= 2 * LT; t++) dp[t] = Real(0);
 #pragma unroll
-    for (int a = 0; a <= 2 * L; a++) {
+    for (int a = 0; a <= LT; a++) {
       if (a > deg[0]) break;
 #pragma unroll
-      for (int c = 0; c <= 2 * L; c++) {
+      for (int c = 0; c <= LT; c++) {
         if (c > deg[1]) break;
         dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
       }
@@ -372,10 +374,10 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
 #pragma unroll
     for (int t = 0; t <= NF; t++) d1[t] = Real(0);
 #pragma unroll
-    for (int a = 0; a <= 4 * L; a++) {
+    for (int a = 0; a <= 2 * LT; a++) {
       if (a > deg[0] + deg[1] || a > NF) break;
 #pragma unroll
-      for (int c = 0; c <= 2 * L; c++) {
+      for (int c = 0; c <= LT; c++) {
         if (c > deg[2] || a + c > NF) break;
         d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
       }
@@ -392,21 +394,21 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
     // thresholds) as the enumeration of the 3^t combinations, 2^t final contractions instead of 3^t.
     constexpr int NS = 1 << TC;
     constexpr int full = NS - 1;
-    Real Ax[NS][2 * L + 1], Qxy[NS][4 * L + 1];
+    Real Ax[NS][LT + 1], Qxy[NS][2 * LT + 1];
     int dAx[NS], dQ[NS];
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
-      Real I[L + 1][L + 1][2 * L + 1];
+      Real I[L + 1][LK + 1][LT + 1];
       const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
       const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
-      if (S.onec) rys_table_1c<L>(R, S.amax[ax], S.cmax[ax], I);
-      else rys_table<L>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
+      if (S.onec) rys_table_1c<L, LK>(R, S.amax[ax], S.cmax[ax], I);
+      else rys_table<L, LK>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       if (ax == 1) {
 #pragma unroll
         for (int t = 0; t < NS; t++) {
           dQ[t] = -1;
 #pragma unroll
-          for (int m = 0; m <= 4 * L; m++) Qxy[t][m] = Real(0);
+          for (int m = 0; m <= 2 * LT; m++) Qxy[t][m] = Real(0);
         }
       }
 #pragma unroll
@@ -415,12 +417,12 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
         subset_options(S, sa, ob, oc);
         const int da = S.np[0][ax] + S.np[1][ax] + 2 * (ob & 1) + (ob & 2);
         const int dc = S.np[2][ax] + S.np[3][ax] + 2 * (oc & 1) + (oc & 2);
-        Real Aa[2 * L + 1];
-        axis_poly<L>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (L + 1), dc, I, ax == 0, Aa);
+        Real Aa[LT + 1];
+        axis_poly<L, LK>(Pn + (ax * NO + ob) * (L + 1), da, Qn + (ax * NO + oc) * (LK + 1), dc, I, ax == 0, Aa);
         const int dA = da + dc;
         if (ax == 0) {
 #pragma unroll
-          for (int m = 0; m <= 2 * L; m++) Ax[sa][m] = Aa[m];
+          for (int m = 0; m <= LT; m++) Ax[sa][m] = Aa[m];
           dAx[sa] = dA;
         } else if (ax == 1) {
 #pragma unroll
@@ -429,10 +431,10 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
             const int st = sx | sa;
             dQ[st] = max(dQ[st], dAx[sx] + dA);
 #pragma unroll
-            for (int a = 0; a <= 2 * L; a++) {
+            for (int a = 0; a <= LT; a++) {
               if (a > dAx[sx]) break;
 #pragma unroll
-              for (int c = 0; c <= 2 * L; c++) {
+              for (int c = 0; c <= LT; c++) {
                 if (c > dA) break;
                 Qxy[st][a + c] = fma(Aa[c], Ax[sx][a], Qxy[st][a + c]);
               }
@@ -442,11 +444,11 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
           const int st = full ^ sa;
           Real sum = Real(0);
 #pragma unroll
-          for (int c = 0; c <= 2 * L; c++) {
+          for (int c = 0; c <= LT; c++) {
             if (c > dA) break;
             Real g = Real(0);
 #pragma unroll
-            for (int a = 0; a <= 4 * L; a++) {
+            for (int a = 0; a <= 2 * LT; a++) {
               if (a > dQ[st] || a + c > NF) break;
               g = fma(Qxy[st][a], F[a + c], g);
             }
@@ -484,8 +486,11 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
 // is written to self_out[16 * (pair_off + P)] (PrimPair::pad[0] of the pair).  By
 // Cauchy-Schwarz |c_P c_Q (P|Q)| <= S_P S_Q for every primitive quartet.
 // TC: how many of the four functions are r^2-type fits (3 cartesian components sharing
-// exponents), 0..4.
-template <int L, int TC>
+// exponents), 0..4.  LK <= L bounds the per-axis degree of the ket pair (the bra's is L): the
+// instances with LK < L serve quartets one of whose pairs is much lighter than the other, with
+// smaller recursion tables and ket polynomials.  A work entry with bit 62 set is evaluated as
+// (jl|ik), which has the same value, so that its lighter pair becomes the ket.
+template <int L, int TC, int LK = L>
 __global__ void __launch_bounds__(128, 1) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
@@ -494,7 +499,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
     double* __restrict__ self_out, const PrimPairF* __restrict__ ppf) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
-  constexpr int QW = 3 * NO * (L + 1);  // ket polynomial values per ket pair
+  constexpr int QW = 3 * NO * (LK + 1);  // ket polynomial values per ket pair
   extern __shared__ double2 s_raw[];
   PrimPair* s_ket = reinterpret_cast<PrimPair*>(s_raw);
   double* s_q = reinterpret_cast<double*>(s_ket + ktile);
@@ -510,8 +515,11 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
 
   const int64_t w = blockIdx.x / split;
   const int part = blockIdx.x % split;
-  const int64_t q = work[w];
-  const int fi = is[q] - 1, fk = ks[q] - 1, fj = js[q] - 1, fl = ls[q] - 1;
+  const int64_t wq = work[w];
+  const int64_t q = wq & ((int64_t(1) << 62) - 1);
+  const bool swp = (wq >> 62) & 1;  // evaluate (jl|ik)
+  const int fi = (swp ? js[q] : is[q]) - 1, fk = (swp ? ls[q] : ks[q]) - 1;
+  const int fj = (swp ? is[q] : js[q]) - 1, fl = (swp ? ks[q] : ls[q]) - 1;
   const int64_t pb = ss_pair_index(fi, fk), pk = ss_pair_index(fj, fl);
   const int nb = pair_cnt[pb], nk = pair_cnt[pk];
   const PrimPair* bra = pp + pair_off[pb];
@@ -547,7 +555,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
     // recentred ket polynomials, per (ket pair, axis, option), and their FP32 copies
     for (int kk = threadIdx.x; kk < kt; kk += blockDim.x) {
       double* qd = s_q + (size_t)kk * QW;
-      pair_polys<L, T2, double>(S, 1, s_ket[kk], qd);
+      pair_polys<LK, T2, double>(S, 1, s_ket[kk], qd);
       if (fp32_tier) {
         float* qf = s_qf + (size_t)kk * QW;
 #pragma unroll
@@ -626,7 +634,8 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
           pair_polys<L, T2, double>(S, 0, P, Pn);
         }
         const PrimPair& Q = s_ket[ik];
-        const double v = prim_quartet<L, TC, double>(S, view64(P), Pn, view64(Q), s_q + (size_t)ik * QW, s_boys);
+        const double v =
+            prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(Q), s_q + (size_t)ik * QW, s_boys);
         if (self_out) {
           self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
           continue;
@@ -660,7 +669,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
           pair_polys<L, T2, float>(S, 0, P, Pn);
           Pv = view32(P);
         }
-        acc32 += prim_quartet<L, TC, float>(S, Pv, Pn, s_ketf[ik], s_qf + (size_t)ik * QW, s_boys32);
+        acc32 += prim_quartet<L, TC, float, LK>(S, Pv, Pn, s_ketf[ik], s_qf + (size_t)ik * QW, s_boys32);
       }
     }
   }

@@ -15,8 +15,8 @@
 
 namespace ss {
 cudaError_t eri_init_constants();
-void eri_tile(int L, bool t2, int max_cnt, int* ktile, size_t* smem);
-cudaError_t launch_eri_class(int L, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
+void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem);
+cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
@@ -122,14 +122,20 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
                    const double* d_pre, double eps, double* self_out = nullptr) {
-  // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four functions)
-  const int NB = 5 * (SS_MAX_POW + 1);
+  // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
+  // functions) and, for L >= 3, whether the lighter pair has L <= 1 (the light-ket instances;
+  // the quartet is then evaluated as (jl|ik) when (j,l) is the lighter pair: bit 62 of its work
+  // entry).  Bucket index 2 (5 L + tc) + light.
+  const int NB = 2 * 5 * (SS_MAX_POW + 1);
+  const int64_t SWAP = int64_t(1) << 62;
   std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
     int i = qis[t] - 1, k = qks[t] - 1, j = qjs[t] - 1, l = qls[t] - 1;
-    int L = std::max(pair_L(c, i, k), pair_L(c, j, l));
+    const int Lb = pair_L(c, i, k), Lk = pair_L(c, j, l);
+    int L = std::max(Lb, Lk);
     int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
-    bucket[5 * L + nt].push_back(t);
+    const bool light = L >= 3 && std::min(Lb, Lk) <= 1 && !self_out;
+    bucket[2 * (5 * L + nt) + (light ? 1 : 0)].push_back(light && Lk > Lb ? (t | SWAP) : t);
   }
   // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes
   // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 127 ways,
@@ -147,11 +153,13 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                                               std::max<int64_t>(1, (target + cnt - 1) / cnt))
                      : 1;
     int64_t local = 0;
-    for (int64_t t : bucket[bk]) {
+    for (int64_t te : bucket[bk]) {
+      const int64_t t = te & (SWAP - 1);
       slot_of_sel[t] = ((pbase[bk] + local * bsplit[bk]) << SLOT_SPLIT_BITS) | bsplit[bk];
       local++;
-      work.push_back(t);
-      int j = qjs[t] - 1, l = qls[t] - 1;
+      work.push_back(te);
+      const bool swp = (te & SWAP) != 0;
+      const int j = (swp ? qis[t] : qjs[t]) - 1, l = (swp ? qks[t] : qls[t]) - 1;  // the ket pair
       maxk[bk] = std::max(maxk[bk], c->h_pp_cnt[ss_pair_index(j, l)]);
     }
     count[bk] = cnt;
@@ -185,19 +193,20 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   for (size_t oi = 0; oi < order.size() && !launch_rc; oi++) {
     const int bk = order[oi];
     cudaStream_t st = c->eri_stream[oi % ss_ctx::ERI_STREAMS];
-    const int L = bk / 5;
-    const int tc = bk % 5;
+    const int L = (bk / 2) / 5;
+    const int tc = (bk / 2) % 5;
+    const int LK = (bk & 1) ? 1 : L;
     const bool t2 = tc > 0;
     int ktile;
     size_t smem;
-    eri_tile(L, t2, std::max(maxk[bk], 1), &ktile, &smem);
+    eri_tile(LK, t2, std::max(maxk[bk], 1), &ktile, &smem);
     // grid.x is limited to 2^31-1: launch in chunks of quartets
     const int split = bsplit[bk];
     const int64_t chunk = (int64_t)(2147483647 / split);
     for (int64_t s0 = 0; s0 < count[bk]; s0 += chunk) {
       int64_t nq = std::min(chunk, count[bk] - s0);
       dim3 grid((unsigned)(nq * split));
-      cudaError_t e = launch_eri_class(L, tc, grid, ktile, smem, st, c->basis,
+      cudaError_t e = launch_eri_class(L, LK, tc, grid, ktile, smem, st, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
                                        d_qjs, d_qks, d_qls, d_pre, eps, d_partial + pbase[bk] + s0 * split,
