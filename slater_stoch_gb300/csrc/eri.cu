@@ -197,24 +197,32 @@ cudaError_t launch_eri_L3c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, 
 cudaError_t launch_eri_L4c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c3k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
 
 // Kernel instance for class (L, tc) and ket bound LK.  tc: number of r^2-type fits among the
 // four functions (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has
-// L = 4; an instance with a larger L serves any smaller one (degrees are runtime).  LK = 1 < L
-// (L = 3, 4; its r^2-type fits, at most two, all in the bra): the light-ket instances.
+// L = 4; an instance with a larger L serves any smaller one (degrees are runtime).  LK = 1, 2 < L
+// (L = 3, 4): the light-ket instances (a ket with L <= 1 holds no r^2-type fit, one with L = 2 at
+// most one, so tc <= 2 and tc <= 3 there).
 cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
                              double* partial, double* self_out, const PrimPairF* ppf) {
   if (LK < L) {
-    if (LK != 1 || L < 3 || tc > 2) return cudaErrorInvalidValue;
-#define SS_K1(LL, TT)                                                                                          \
-  if (L == LL && tc == TT)                                                                                     \
-    return launch_eri_L##LL##c##TT##k1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, \
-                                       eps, partial, self_out, ppf);
-    SS_K1(3, 0) SS_K1(3, 1) SS_K1(3, 2) SS_K1(4, 0) SS_K1(4, 1) SS_K1(4, 2)
-#undef SS_K1
+#define SS_KV(LL, TT, KK)                                                                                       \
+  if (L == LL && tc == TT && LK == KK)                                                                          \
+    return launch_eri_L##LL##c##TT##k##KK(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, \
+                                          pre, eps, partial, self_out, ppf);
+    SS_KV(3, 0, 1) SS_KV(3, 1, 1) SS_KV(3, 2, 1) SS_KV(4, 0, 1) SS_KV(4, 1, 1) SS_KV(4, 2, 1)
+    SS_KV(3, 0, 2) SS_KV(3, 1, 2) SS_KV(3, 2, 2) SS_KV(4, 0, 2) SS_KV(4, 1, 2) SS_KV(4, 2, 2) SS_KV(4, 3, 2)
+#undef SS_KV
     return cudaErrorInvalidValue;
   }
   if (tc == 0) {

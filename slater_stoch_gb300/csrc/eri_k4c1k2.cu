@@ -1,0 +1,18 @@
+// eri_k4c1k2.cu -- eri_kernel<4, 1, 2>: class (4, 1) quartets whose lighter pair has per-axis
+// degree <= 2, evaluated with that pair as the ket (own translation unit).
+#include "eri_kernel.cuh"
+
+namespace ss {
+cudaError_t launch_eri_L4c1k2(dim3 grid, int ktile, size_t smem, cudaStream_t st, const BasisDev& B,
+                                  const PrimPair* pp, const int64_t* off, const int* cnt, const int64_t* work,
+                                  int split, const int32_t* is, const int32_t* js, const int32_t* ks,
+                                  const int32_t* ls, const double* pre, double eps, double* partial,
+                                  double* self_out, const PrimPairF* ppf) {
+  cudaError_t e =
+      cudaFuncSetAttribute(eri_kernel<4, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  eri_kernel<4, 1, 2><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, pre, eps,
+                                                  partial, self_out, ppf);
+  return cudaGetLastError();
+}
+}  // namespace ss

@@ -123,10 +123,10 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
                    const double* d_pre, double eps, double* self_out = nullptr) {
   // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
-  // functions) and, for L >= 3, whether the lighter pair has L <= 1 (the light-ket instances;
-  // the quartet is then evaluated as (jl|ik) when (j,l) is the lighter pair: bit 62 of its work
-  // entry).  Bucket index 2 (5 L + tc) + light.
-  const int NB = 2 * 5 * (SS_MAX_POW + 1);
+  // functions) and, for L >= 3, the light-ket variant v: the lighter pair has L <= v (v = 1, 2;
+  // v = 0 for the others).  A light-ket quartet is evaluated as (jl|ik) when (j,l) is the
+  // lighter pair (bit 62 of its work entry).  Bucket index 3 (5 L + tc) + v.
+  const int NB = 3 * 5 * (SS_MAX_POW + 1);
   const int64_t SWAP = int64_t(1) << 62;
   std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
@@ -134,8 +134,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     const int Lb = pair_L(c, i, k), Lk = pair_L(c, j, l);
     int L = std::max(Lb, Lk);
     int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
-    const bool light = L >= 3 && std::min(Lb, Lk) <= 1 && !self_out;
-    bucket[2 * (5 * L + nt) + (light ? 1 : 0)].push_back(light && Lk > Lb ? (t | SWAP) : t);
+    const int lmin = std::min(Lb, Lk);
+    const int v = (L >= 3 && lmin <= 2 && !self_out) ? std::max(lmin, 1) : 0;
+    bucket[3 * (5 * L + nt) + v].push_back(v && Lk > Lb ? (t | SWAP) : t);
   }
   // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes
   // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 127 ways,
@@ -193,9 +194,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   for (size_t oi = 0; oi < order.size() && !launch_rc; oi++) {
     const int bk = order[oi];
     cudaStream_t st = c->eri_stream[oi % ss_ctx::ERI_STREAMS];
-    const int L = (bk / 2) / 5;
-    const int tc = (bk / 2) % 5;
-    const int LK = (bk & 1) ? 1 : L;
+    const int L = (bk / 3) / 5;
+    const int tc = (bk / 3) % 5;
+    const int LK = (bk % 3) ? bk % 3 : L;
     const bool t2 = tc > 0;
     int ktile;
     size_t smem;
