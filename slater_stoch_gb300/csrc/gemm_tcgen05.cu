@@ -312,7 +312,7 @@ extern "C" int ss_split_bf16_gemm_noalloc(void* stream, int P, int64_t K, const 
   SS_CUDA_TRY(cudaGetDevice(&dev));
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (ksplit == 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(K / 64, (2 * sms + T * T - 1) / (T * T)));
+  if (ksplit == 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(K / 64, (2 * sms) / (T * T)));
   ksplit = (int)std::min<size_t>((size_t)ksplit, cap / PP);
   if (dev < 0 || dev >= 64) {
     ss_set_error_msg("ss_split_bf16_gemm_noalloc: device %d out of range", dev);
