@@ -21,7 +21,7 @@ EXEC_FLOPS_PER_PRIM = 241.5
 
 # workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job
 EXEC_FLOPS = {
-    "h2o_26_ng20": (8.3372e11, 3.3122e11),
+    "h2o_26_ng20": (8.2948e11, 3.3580e11),
 }
 
 
