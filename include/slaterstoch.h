@@ -199,7 +199,7 @@ int ss_davidson(ss_ctx* ctx, const double* moy, int layout, int m, double tol, i
 /* Matrix-free removal of the negative eigencomponents (replaces the nbasis >= 200 path of
  * davidson_clean, src/davidson_clean.F90:120-323): the ERI matrix in `layout` is applied from
  * the unique quartet values only (never formed); block Davidson for the lowest `block` Ritz
- * pairs (<= 128; 0 = nbasis, the reference's mmax) in a basis of at most block x max_blocks
+ * pairs (<= 128; 0 = min(nbasis, 128), the reference's mmax) in a basis of at most block x max_blocks
  * vectors (0 = nbasis, the reference's NMAX; capped at the matrix dimension and 1024); each
  * search ends when the Ritz pairs up to index block/2 and all negative ones have residual
  * norm < tol (or the basis spans the whole space); its negative pairs are deflated,

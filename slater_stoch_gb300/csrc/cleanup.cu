@@ -747,7 +747,9 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
     return SS_ERR_ARG;
   }
   const int N = (int)N64;
-  if (m <= 0) m = n;  // src/davidson_clean.F90:129-131: mmax = NMAX = nbasis
+  // src/davidson_clean.F90:129-131: mmax = NMAX = nbasis; the default block is capped at the
+  // MF_MAXM columns one product handles (a caller asking for more gets SS_ERR_UNSUPPORTED)
+  if (m <= 0) m = std::min(n, MF_MAXM);
   if (nmax <= 0) nmax = n;
   m = std::min(m, std::max(1, N / 2));
   if (m > MF_MAXM) {
