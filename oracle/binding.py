@@ -2,9 +2,9 @@
 bench.py's CPU-baseline leg only; the product never imports this module).
 
 Restates the reference's algorithms (scemama/slater_stoch); see ss_oracle.c for
-the file:line each function follows.  Parity status: pinned by analytic
-known-answer tests only -- the reference has no golden outputs and cannot be
-compiled in this environment.
+the file:line each function follows.  Parity status: parity unpinned -- the
+reference has no golden outputs and cannot be compiled in this environment; the
+oracle is checked against analytic known-answer tests only.
 """
 from __future__ import annotations
 

@@ -8,6 +8,9 @@ baseline only).  numpy restatements of the reference:
   (``philox4x32_10`` below, Salmon et al. SC'11), so both sides project on the same
   subspaces; the reference's Fortran random_number stream cannot be reproduced.
 * ``davidson``   -- src/davidson.F90:1-158 with the generalized projected problem (dsygv).
+
+Parity status: parity unpinned (the reference's LAPACK/BLAS are unpinned and it cannot be run
+here); the gates are PSD-ness and agreement with numpy's eigensolvers.
 """
 from __future__ import annotations
 

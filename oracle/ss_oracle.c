@@ -7,9 +7,10 @@
  * Built with -ffp-contract=off so no fused multiply-adds change the rounding
  * of the reference's expressions.
  *
- * Parity status: the reference has no tests or golden outputs and cannot be
- * compiled here (Fortran, no compiler); this oracle is pinned by analytic
- * known-answer tests (see tests/test_oracle_kat.py).
+ * Parity status: parity unpinned.  The reference has no tests or golden outputs
+ * and cannot be compiled here (Fortran, no compiler), so nothing of the
+ * reference's own pins this restatement; it is checked instead against
+ * analytic known-answer tests (closed forms, quadrature; tests/test_oracle_kat.py).
  *
  * Known, documented deviations from the reference's arithmetic:
  *  - fact(n) (src/fact.F90:1-27) returns exp(logfact(n)) on the first call

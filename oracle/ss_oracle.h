@@ -12,10 +12,12 @@
  *   - shared-walker estimator in FP64 (the exact arithmetic the split-BF16
  *     GEMM path approximates; no reference counterpart, see shared_* below)
  *
- * Parity status: the reference ships no tests and no expected outputs and
- * cannot be compiled in this environment (Fortran).  The oracle is pinned by
- * analytic known-answer tests (closed-form s-Gaussian ERIs, Boys function
- * against quadrature, the STO 1s self-repulsion 5*pi^2/(8 zeta^5)).
+ * Parity status: parity unpinned.  The reference ships no tests and no
+ * expected outputs and cannot be compiled in this environment (Fortran), so no
+ * output of the reference pins the oracle; it is checked against analytic
+ * known-answer tests instead (closed-form s-Gaussian ERIs, Boys function
+ * against quadrature, the STO 1s self-repulsion 5*pi^2/(8 zeta^5), closed-form
+ * one-centre Slater integrals and one-electron integrals).
  *
  * Array layouts follow the reference's Fortran column-major arrays with
  * 0-based indices: center(3,n) -> center[l + 3*i]; npower(3,n) likewise;
