@@ -203,6 +203,7 @@ def main():
     import torch.distributed as dist
     from slater_stoch_gb300 import api
     from slater_stoch_gb300.perfmodel import eri_fp64_flops
+    from slater_stoch_gb300.replicas import job_seed, max_over_ranks, whole_job_throughput
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -220,7 +221,7 @@ def main():
     ctx.set_quartets(*q)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
-    seed = 1 + rank
+    seed = job_seed(1, rank)
 
     def job():
         ctx.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=False)
@@ -253,11 +254,8 @@ def main():
         t_wall = time.perf_counter() - t_wall0
     launches = (ctx.launches - l0) // max(args.steps, 1)
     max_sigma = ctx.max_sigma
-    tmax = torch.tensor([sum(times)], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    ms_step = float(tmax.item()) / args.steps
-    value = world * nint / (ms_step * 1e-3)
+    ms_step = max_over_ranks(sum(times), world, dist, dev) / args.steps
+    value = whole_job_throughput(nint, world, ms_step * 1e-3)
 
     # end-to-end through the C ABI with host buffers: upload basis + quartets, copy results back
     e2e_times = []
@@ -271,6 +269,7 @@ def main():
         eri, sig = c2.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=True)
         e2e_times.append(time.perf_counter() - t)
         c2.close()
+    e2e_s = max_over_ranks(statistics.median(e2e_times), world, dist, dev)  # the slowest rank's job
     h2d = sum(a.nbytes for a in ctx._basis_arrays) + 4 * 4 * nint
     d2h = 2 * 8 * nint
 
@@ -355,7 +354,7 @@ def main():
             "fp64_plain": {"value": plain_value, "unit": "ERIs/s", "analytic_s": t_analytic,
                            "mc_s_scaled": t_plain_mc, "measured_walkers": plain_npts,
                            "speedup_split_bf16_vs_fp64_plain": value / world / plain_value},
-            "e2e": {"value": world * nint / statistics.median(e2e_times), "unit": "ERIs/s",
+            "e2e": {"value": whole_job_throughput(nint, world, e2e_s), "unit": "ERIs/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "roofline": roofline,
