@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "ss_common.cuh"
@@ -186,9 +187,13 @@ __global__ void combine_mono_kernel(int64_t nint, const double* __restrict__ g, 
   }
 }
 
+// once per device and process; job worker threads may get here together
+static std::mutex g_tables_mu;
+static bool g_tables_done[64] = {false};
+
 static int upload_tables(ss_ctx* c) {
-  static bool done_dev[64] = {false};
-  if (c->device >= 0 && c->device < 64 && done_dev[c->device]) return SS_OK;
+  std::lock_guard<std::mutex> lock(g_tables_mu);
+  if (c->device >= 0 && c->device < 64 && g_tables_done[c->device]) return SS_OK;
   double f[MC_FACT];
   f[0] = 1.0;
   for (int i = 1; i < MC_FACT; i++) f[i] = f[i - 1] * i;
@@ -226,7 +231,7 @@ static int upload_tables(ss_ctx* c) {
   SS_CUDA_TRY(cudaMemcpyToSymbolAsync(c_ylm_re, re, sizeof re, 0, cudaMemcpyHostToDevice, c->stream));
   SS_CUDA_TRY(cudaMemcpyToSymbolAsync(c_ylm_im, im, sizeof im, 0, cudaMemcpyHostToDevice, c->stream));
   SS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  if (c->device >= 0 && c->device < 64) done_dev[c->device] = true;
+  if (c->device >= 0 && c->device < 64) g_tables_done[c->device] = true;
   return SS_OK;
 }
 
