@@ -523,7 +523,6 @@ int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, i
   bool converged = false;
   int total = 0;
   while (!converged && total < max_iter) {
-    int cols = m;  // columns of U in use
     for (int iter = 1; iter <= nmax - 1 && !converged && total < max_iter; iter++, total++) {
       const int shift = m * (iter - 1);
       // W(:, shift:shift+m) = H U(:, shift:shift+m)
@@ -572,9 +571,7 @@ int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, i
         CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &mone, U, N, tmp, k, &one, Un, N));
       }
       TRY(ortho_qr(st, N, m, Un, N, Qw, tau, &c->launches));
-      cols = k + m;
     }
-    (void)cols;
     // restart with the current Ritz vectors (src/davidson.F90:151-155)
     SS_CUDA_TRY(cudaMemcpyAsync(U, X, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, st));
     TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
