@@ -135,6 +135,17 @@ int ss_job_submit(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_b
 int ss_job_poll(ss_ctx* ctx, int64_t job_id, int* done);
 int ss_job_result(ss_ctx* ctx, int64_t job_id, double* eri, double* sigma);
 
+/* Admission of the asynchronous jobs of this context: a job starts in submission order once
+ * fewer than max_running jobs run (0 = no limit) and its ERI-buffer footprint,
+ * ss_job_footprint(nint), fits in what the running jobs leave of eri_budget_bytes (0 = no
+ * limit); a job starts regardless when no other job runs.  ss_job_submit refuses a job whose
+ * footprint alone exceeds the budget (SS_ERR_NOMEM). */
+int ss_job_limits(ss_ctx* ctx, size_t eri_budget_bytes, int max_running);
+/* running / queued jobs now, the most that ran at once and their largest summed footprint */
+int ss_job_stats(ss_ctx* ctx, int* running, int* queued, int* peak_running, size_t* peak_bytes);
+/* device bytes per job that grow with its quartet count (96 per quartet) */
+size_t ss_job_footprint(int64_t nint);
+
 /* Drop cached device results (Schwarz diagonal, analytic ERIs, MC sums); inputs stay. */
 int ss_invalidate(ss_ctx* ctx);
 

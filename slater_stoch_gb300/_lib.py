@@ -45,6 +45,9 @@ SIGNATURES = {
                                 C.c_double, C.c_void_p]),
     "ss_job_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "ss_job_result": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "ss_job_limits": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
+    "ss_job_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ss_job_footprint": (C.c_size_t, [C.c_int64]),
     "ss_nuclei_set": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p]),
     "ss_one_e": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ss_write_bielec_ao": (C.c_int, [C.c_void_p, C.c_char_p]),

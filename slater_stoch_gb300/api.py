@@ -193,6 +193,21 @@ class Context:
         _lib.check(self._L.ss_job_result(self._h, int(job_id), _ptr(eri), _ptr(sig)))
         return eri, sig
 
+    def job_limits(self, eri_budget_bytes: int = 0, max_running: int = 0):
+        """Admit this context's jobs in submission order within an ERI-buffer budget (bytes,
+        0 = none) and a number of concurrent jobs (0 = none)."""
+        _lib.check(self._L.ss_job_limits(self._h, int(eri_budget_bytes), int(max_running)))
+
+    def job_stats(self) -> dict:
+        v = [np.zeros(1, np.int32) for _ in range(3)] + [np.zeros(1, np.uint64)]
+        _lib.check(self._L.ss_job_stats(self._h, *[_ptr(a) for a in v]))
+        return {"running": int(v[0][0]), "queued": int(v[1][0]), "peak_running": int(v[2][0]),
+                "peak_bytes": int(v[3][0])}
+
+    def job_footprint(self) -> int:
+        """Device bytes of this context's quartet count by which its jobs are admitted."""
+        return int(self._L.ss_job_footprint(int(self.nint)))
+
     def invalidate(self):
         _lib.check(self._L.ss_invalidate(self._h))
 

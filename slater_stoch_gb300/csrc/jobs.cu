@@ -5,7 +5,9 @@
 // copies the context's basis and quartet list at submit time, then runs on a worker thread with
 // a private context (its own stream and device buffers) on the same device, so jobs of one
 // context overlap each other and later changes to the submitting context do not affect them.
-// Results are kept in host memory until ss_job_result collects them.
+// Results are kept in host memory until ss_job_result collects them.  Jobs are admitted in
+// submission order by their ERI-buffer footprint and a concurrency limit (ss_job_limits,
+// admission.h): a worker thread waits for its turn before it creates its context.
 #include <string.h>
 
 #include <atomic>
@@ -54,6 +56,14 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
     ss_set_error_msg("ss_job_submit needs ss_basis_set and ss_quartets_set first");
     return SS_ERR_STATE;
   }
+  if (!c->admission) c->admission = std::make_shared<JobAdmission>();
+  const size_t foot = JOB_BYTES_PER_QUARTET * (size_t)c->nint;
+  const int64_t ticket = c->admission->enqueue(foot);
+  if (ticket < 0) {
+    ss_set_error_msg("ss_job_submit: the job's ERI buffers (%zu bytes) exceed the job budget", foot);
+    return SS_ERR_NOMEM;
+  }
+  std::shared_ptr<JobAdmission> adm = c->admission;
   auto js = std::make_shared<JobState>();
   js->eri.assign(c->nint, 0.0);
   js->sigma.assign(c->nint, 0.0);
@@ -68,6 +78,7 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
   JobState* st = js.get();
   try {
     js->th = std::thread([=]() {
+      adm->admit(ticket, foot);
       ss_ctx* w = ss_create(device, budget);
       int rc = w ? SS_OK : SS_ERR_CUDA;
       if (!rc)
@@ -84,9 +95,11 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
       }
       st->rc = rc;
       if (w) ss_destroy(w);
+      adm->release(foot);
       st->done.store(1);
     });
   } catch (const std::exception& ex) {
+    adm->abandon(ticket);
     ss_set_error_msg("ss_job_submit: cannot start a worker thread (%s)", ex.what());
     return SS_ERR_STATE;
   }
@@ -132,5 +145,31 @@ int ss_job_result(ss_ctx* c, int64_t job_id, double* eri, double* sigma) {
   if (sigma) memcpy(sigma, js->sigma.data(), bytes);
   return SS_OK;
 }
+
+int ss_job_limits(ss_ctx* c, size_t eri_budget_bytes, int max_running) {
+  if (!c || max_running < 0) {
+    ss_set_error_msg("ss_job_limits: bad arguments");
+    return SS_ERR_ARG;
+  }
+  if (!c->admission) c->admission = std::make_shared<JobAdmission>();
+  c->admission->set_limits(eri_budget_bytes, max_running);
+  return SS_OK;
+}
+
+int ss_job_stats(ss_ctx* c, int* running, int* queued, int* peak_running, size_t* peak_bytes) {
+  if (!c) {
+    ss_set_error_msg("null context");
+    return SS_ERR_ARG;
+  }
+  JobAdmission::Stats s;
+  if (c->admission) s = c->admission->stats();
+  if (running) *running = s.running;
+  if (queued) *queued = s.queued;
+  if (peak_running) *peak_running = s.peak_running;
+  if (peak_bytes) *peak_bytes = s.peak_used;
+  return SS_OK;
+}
+
+size_t ss_job_footprint(int64_t nint) { return nint > 0 ? JOB_BYTES_PER_QUARTET * (size_t)nint : 0; }
 
 }  // extern "C"

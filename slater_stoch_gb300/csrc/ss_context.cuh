@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "admission.h"
 #include "ss_common.cuh"
 
 namespace ss {
@@ -92,8 +93,9 @@ struct ss_ctx {
   bool have_mc = false;
   bool have_resid = false;  // shared-walker residual tables of the current basis (pool "rs_*")
 
-  // asynchronous jobs (jobs.cu)
+  // asynchronous jobs (jobs.cu) and their admission (admission.h)
   std::map<int64_t, std::shared_ptr<ss::JobState>> jobs;
+  std::shared_ptr<ss::JobAdmission> admission;
   int64_t next_job = 1;
   ss::DevBuf d_mean, d_sigma;
 

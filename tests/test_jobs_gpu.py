@@ -51,3 +51,25 @@ def test_job_errors_are_reported():
             ctx.job_result(jid)
         with pytest.raises(SSError, match="unknown job"):
             ctx.job_poll(jid)
+
+
+def test_job_admission_limits():
+    """Jobs admitted one at a time (max_running = 1) reproduce the synchronous job and never
+    overlap; a job whose ERI-buffer footprint exceeds the budget is refused at submission."""
+    b = configs.h2o_minimal(ng0=6)
+    q = basis.build_mapping(b.n)
+    args = dict(a_zv=1.8, npts=8192, nblocks=2, estimator="shared", precision="split_bf16")
+    with _ctx(b, q) as ctx:
+        foot = ctx.job_footprint()
+        assert foot == 96 * len(q[0])
+        ctx.job_limits(max_running=1)
+        ids = [ctx.job_submit(seed=s, **args) for s in (3, 4, 5)]
+        res = [ctx.job_result(i) for i in ids]
+        st = ctx.job_stats()
+        assert st["peak_running"] == 1 and st["running"] == 0 and st["queued"] == 0
+        assert st["peak_bytes"] == foot
+        ref = ctx.two_e_job(seed=5, **args)
+        np.testing.assert_allclose(res[2][0], ref[0], rtol=1e-14, atol=1e-17)
+        ctx.job_limits(eri_budget_bytes=foot // 2)
+        with pytest.raises(SSError, match="budget"):
+            ctx.job_submit(seed=6, **args)
