@@ -9,7 +9,7 @@ negative eigenvalues (as MC noise does).  Both sides draw the same Philox test m
   edge for components whose +/- partners are nearly degenerate (they are noise-level), so the
   two agree to the perturbation's size; both reduce the negative part.
 * exact projection: matches the oracle to 1e-12 of the largest ERI, and with the packed
-  Coulomb metric the cleaned matrix is PSD to -1e-12 (the benchmark spec gate).
+  Coulomb metric the cleaned matrix is PSD to -1e-12 (the PSD gate of the cleanup).
 * Davidson: lowest 10 eigenvalues against numpy.linalg.eigh to 1e-8 of the spectrum.
 """
 import numpy as np
@@ -92,8 +92,8 @@ def test_psd_project_rank_deficient_metric():
 
 
 def test_clean_pipeline_is_psd():
-    """svd_clean (the benchmark spec parameters: rank 200, oversampling 10, 4 power iterations on the
-    351x351 packed metric) followed by the exact projection: PSD to -1e-12."""
+    """svd_clean with the 26-function workload's parameters (rank 200, oversampling 10, 4 power
+    iterations on the 351x351 packed metric) followed by the exact projection: PSD to -1e-12."""
     from oracle import cleanup as OC
     b, q, g, moy = _noisy_eris("h2o_26", 6, "packed_pair")
     with api.Context(0) as ctx:

@@ -1,6 +1,6 @@
 """GPU analytic Gaussian-fit ERIs vs the CPU oracle (restated gauss_ijkl, src/gauss_ijkl.F90).
 
-Tolerance (the benchmark spec: analytic Gaussian ERIs to 1e-12): per integral
+Tolerance (analytic Gaussian ERIs to 1e-12): per integral
 |gpu - oracle| <= 1e-12 * |oracle| + 1e-12 * sqrt(precond_ik * precond_jl),
 the second term covers integrals that vanish by symmetry (both sides are ~1e-20).
 """

@@ -7,7 +7,7 @@ the correction and S_q = sqrt((ik|ik)(jl|jl)) the Schwarz bound (the magnitude o
 accumulated STO and fit sums, whose FP64 rounding limits a correction that is their difference).
 
 Shared estimator, split-BF16 tensor-core contraction: the oracle evaluates the same
-estimator in FP64 on the same samples (u1, u2, w).  Gate (the benchmark spec): per integral
+estimator in FP64 on the same samples (u1, u2, w).  Gate: per integral
 |gpu - fp64| <= 0.1 sigma_MC and <= 1e-8 Ha.
 """
 import numpy as np
