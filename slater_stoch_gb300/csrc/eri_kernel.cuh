@@ -27,6 +27,24 @@
 #include "boys.cuh"
 #include "ss_common.cuh"
 
+// The per-primitive-quartet arithmetic below is plain IEEE arithmetic with explicit fma, so it
+// also compiles as host C++ (the host build of the tests checks it against the oracle); the
+// kernel itself is device-only.
+#ifdef __CUDACC__
+#define SS_DFI __device__ __forceinline__
+#else
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#define SS_DFI inline
+using std::fma;
+using std::max;
+using std::min;
+inline double rsqrt(double x) { return 1.0 / std::sqrt(x); }
+inline float rsqrt(float x) { return 1.0f / std::sqrt(x); }
+#endif
+
 namespace ss {
 
 constexpr double THRESH = 1.e-15;
@@ -36,7 +54,7 @@ constexpr double PI_5_2 = 34.9868366552;  // src/general_primitive_integral.F90:
 // (src/give_explicit_poly_and_gaussian.F90:86-220, cases 0..4; the powers and the exact
 // integer binomials of each case)
 template <int L, typename Real>
-__device__ __forceinline__ void recentered(Real pw1, int a, Real (&P)[L + 1]) {
+SS_DFI void recentered(Real pw1, int a, Real (&P)[L + 1]) {
 #pragma unroll
   for (int t = 0; t <= L; t++) P[t] = Real(0);
   if (a == 0) {
@@ -64,7 +82,7 @@ __device__ __forceinline__ void recentered(Real pw1, int a, Real (&P)[L + 1]) {
 
 // P_new = recentered(A,a) * recentered(B,b) in multiply_poly's order (src/multiply_poly.F90:22-31)
 template <int L, typename Real>
-__device__ __forceinline__ void pair_poly(Real pa, int a, Real pb, int b, Real* Pn) {
+SS_DFI void pair_poly(Real pa, int a, Real pb, int b, Real* Pn) {
   Real Pa[L + 1], Pb[L + 1];
   recentered<L, Real>(pa, a, Pa);
   recentered<L, Real>(pb, b, Pb);
@@ -86,7 +104,7 @@ struct RecCoefT {
 // the same per-coefficient operation order as I_x1_pol_mult / I_x2_pol_mult:
 //   I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1);  I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
 template <int L, int LK, typename Real>
-__device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int cmax,
+SS_DFI void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int cmax,
                                           Real (&I)[L + 1][LK + 1][L + LK + 1]) {
 #pragma unroll
   for (int c = 0; c <= LK; c++) {
@@ -133,7 +151,7 @@ __device__ __forceinline__ void rys_table(const RecCoefT<Real>& R, Real Cc, Real
 // The same table when bra and ket share one centre (all four functions on one atom): C00 and
 // D00 vanish, so only the B10/B01/B00 terms remain and every entry with a + c odd is zero.
 template <int L, int LK, typename Real>
-__device__ __forceinline__ void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
+SS_DFI void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
                                              Real (&I)[L + 1][LK + 1][L + LK + 1]) {
 #pragma unroll
   for (int c = 0; c <= LK; c++) {
@@ -176,19 +194,24 @@ __device__ __forceinline__ void rys_table_1c(const RecCoefT<Real>& R, int amax, 
 }
 
 // |x| < t and |x| > t on the bit patterns (integer pipe; x finite, t > 0)
-__device__ __forceinline__ bool abs_lt(double x, double t) {
-  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(t);
+SS_DFI int32_t fbits_of(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_int(x);
+#else
+  int32_t v;
+  memcpy(&v, &x, sizeof v);
+  return v;
+#endif
 }
-__device__ __forceinline__ bool abs_gt(double x, double t) {
-  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(t);
-}
-__device__ __forceinline__ bool abs_lt(float x, float t) { return (__float_as_int(x) & 0x7FFFFFFF) < __float_as_int(t); }
-__device__ __forceinline__ bool abs_gt(float x, float t) { return (__float_as_int(x) & 0x7FFFFFFF) > __float_as_int(t); }
+SS_DFI bool abs_lt(double x, double t) { return (bits_of(x) & 0x7FFFFFFFFFFFFFFFLL) < bits_of(t); }
+SS_DFI bool abs_gt(double x, double t) { return (bits_of(x) & 0x7FFFFFFFFFFFFFFFLL) > bits_of(t); }
+SS_DFI bool abs_lt(float x, float t) { return (fbits_of(x) & 0x7FFFFFFF) < fbits_of(t); }
+SS_DFI bool abs_gt(float x, float t) { return (fbits_of(x) & 0x7FFFFFFF) > fbits_of(t); }
 
 // Ix = sum_{ix,jx} (Pn[ix] Qn[jx]) I(ix,jx) with the thresholds of general_primitive_integral
 // (x axis: skip |P| < thresh; y, z: keep |P| > thresh; skip |P Q| < thresh).
 template <int L, int LK, typename Real>
-__device__ __forceinline__ void axis_poly(const Real* Pn, int degP, const Real* Qn, int degQ,
+SS_DFI void axis_poly(const Real* Pn, int degP, const Real* Qn, int degQ,
                                           const Real (&I)[L + 1][LK + 1][L + LK + 1], bool x_axis,
                                           Real* out) {
 #pragma unroll
@@ -222,7 +245,7 @@ struct QuartetShape {
 };
 
 template <bool T2>
-__device__ __forceinline__ QuartetShape quartet_shape(const BasisDev& B, int fi, int fk, int fj, int fl) {
+SS_DFI QuartetShape quartet_shape(const BasisDev& B, int fi, int fk, int fj, int fl) {
   QuartetShape S;
   const int fn[4] = {fi, fk, fj, fl};
   S.nf = 0;
@@ -259,7 +282,7 @@ __device__ __forceinline__ QuartetShape quartet_shape(const BasisDev& B, int fi,
 // Which functions of the quartet take the +2 of their r^2 fit on one axis, for a subset s of
 // the r^2-type functions (bit b of s = function tf[b]): bra option ob (bit0 = i, bit1 = k), ket
 // option oc (bit0 = j, bit1 = l), as used by pair_polys.
-__device__ __forceinline__ void subset_options(const QuartetShape& S, int s, int& ob, int& oc) {
+SS_DFI void subset_options(const QuartetShape& S, int s, int& ob, int& oc) {
   int plus[4] = {0, 0, 0, 0};
 #pragma unroll
   for (int b = 0; b < 4; b++)
@@ -271,7 +294,7 @@ __device__ __forceinline__ void subset_options(const QuartetShape& S, int s, int
 // recentred pair polynomials of a primitive pair, per (axis, option); side 0 = bra (functions
 // i, k), side 1 = ket (functions j, l).  Layout [ax][o][L+1].
 template <int L, bool T2, typename Real, typename Rec>
-__device__ __forceinline__ void pair_polys(const QuartetShape& S, int side, const Rec& P, Real* out) {
+SS_DFI void pair_polys(const QuartetShape& S, int side, const Rec& P, Real* out) {
   constexpr int NO = T2 ? 4 : 1;
   const int f0 = 2 * side, f1 = 2 * side + 1;
 #pragma unroll
@@ -292,13 +315,13 @@ struct PairView {
   Real p, p_inv, P[3], fact;
 };
 
-__device__ __forceinline__ PairView<double> view64(const PrimPair& A) {
+SS_DFI PairView<double> view64(const PrimPair& A) {
   return PairView<double>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fact};
 }
 
 // FP32 view: fact carries K_AB times the coefficient product, so the FP32 quartet value comes
 // out already multiplied by the coefficients
-__device__ __forceinline__ PairView<float> view32(const PrimPairF& A) {
+SS_DFI PairView<float> view32(const PrimPairF& A) {
   return PairView<float>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fc};
 }
 
@@ -309,7 +332,7 @@ __device__ __forceinline__ PairView<float> view32(const PrimPairF& A) {
 // over the axes below).  L bounds the per-axis degree of the bra pair, LK that of the ket pair
 // (Pn: [ax][o][L+1], Qn: [ax][o][LK+1]); the total degree is at most 3 (L + LK).
 template <int L, int TC, typename Real, int LK = L>
-__device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const Real* Pn,
+SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const Real* Pn,
                                              const PairView<Real>& Q, const Real* Qn, const Real* s_boys) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;
@@ -464,6 +487,7 @@ __device__ __forceinline__ Real prim_quartet(const QuartetShape& S, const PairVi
   return pref * accu;
 }
 
+#ifdef __CUDACC__
 // Work per CTA: one function quartet (ik|jl) and a slice of its bra primitive pairs against all
 // its ket primitive pairs, the ket pairs staged in shared memory in tiles together with their
 // recentred polynomials.
@@ -681,5 +705,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
   __syncthreads();
   if (threadIdx.x == 0) partial[w * split + part] = ((s_red[0] + s_red[1]) + s_red[2]) + s_red[3];
 }
+
+#endif  // __CUDACC__
 
 }  // namespace ss

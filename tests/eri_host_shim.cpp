@@ -1,0 +1,184 @@
+// Host build of the analytic ERI kernel's arithmetic (slater_stoch_gb300/csrc/eri_kernel.cuh):
+// the contracted ERI of each quartet from the kernel's own templates (pair_polys, prim_quartet,
+// the Boys tables), with the device's choice of template instance and light-ket orientation,
+// over all primitive pairs (no screening, FP64 only).  The primitive pairs are built as
+// prim_pair_fill builds them (csrc/eri.cu), including the folding of same-fit pairs.
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "../slater_stoch_gb300/csrc/eri_kernel.cuh"
+
+using namespace ss;
+
+namespace {
+
+const double* boys_tables() {
+  static std::vector<double> t;
+  if (t.empty()) {
+    t.insert(t.end(), boys_hi_tab, boys_hi_tab + BOYS_HI_K * BOYS_HI_J);
+    t.insert(t.end(), boys_lo_tab, boys_lo_tab + BOYS_LO_K * BOYS_LO_N);
+    t.insert(t.end(), exp2_32_tab, exp2_32_tab + 32);
+  }
+  return t.data();
+}
+
+bool fold_pair_h(const BasisDev& B, int i, int k) {
+  if (i == k) return true;
+  const int ng = B.n_gauss[i];
+  if (ng != B.n_gauss[k] || B.i_type[i] != B.i_type[k]) return false;
+  for (int ax = 0; ax < 3; ax++)
+    if (B.center[3 * i + ax] != B.center[3 * k + ax]) return false;
+  const int64_t t = B.i_type[i] == 2 ? 1 : 0;
+  for (int m = 0; m < ng; m++) {
+    if (B.g_gauss[m + (int64_t)B.ld * i] != B.g_gauss[m + (int64_t)B.ld * k]) return false;
+    if (B.c_gauss[m + (int64_t)B.ld * (i + B.n * t)] != B.c_gauss[m + (int64_t)B.ld * (k + B.n * t)]) return false;
+  }
+  return true;
+}
+
+std::vector<PrimPair> build_pairs(const BasisDev& B, int i, int k, bool fold_enabled) {
+  std::vector<PrimPair> out;
+  const int ngi = B.n_gauss[i], ngk = B.n_gauss[k];
+  const double* A = B.center + 3 * i;
+  const double* Bc = B.center + 3 * k;
+  const int ti = B.i_type[i] == 2 ? 1 : 0, tk = B.i_type[k] == 2 ? 1 : 0;
+  const bool fold = fold_enabled && fold_pair_h(B, i, k);
+  for (int m1 = 0; m1 < ngi; m1++)
+    for (int m2 = (fold ? m1 : 0); m2 < ngk; m2++) {
+      const double a = B.g_gauss[m1 + (int64_t)B.ld * i], b = B.g_gauss[m2 + (int64_t)B.ld * k];
+      const double p = a + b;
+      const double p_inv = 1.0 / (a + b);
+      double ab = a * b;
+      const double x0 = A[0] - Bc[0], x1 = A[1] - Bc[1], x2 = A[2] - Bc[2];
+      ab = ab * p_inv;
+      const double kk = ab * (x0 * x0 + x1 * x1 + x2 * x2);
+      if (kk > 40.0) continue;
+      const double K = std::exp(-kk);
+      if (K < 1.e-15) continue;
+      PrimPair r{};
+      r.p = p;
+      r.p_inv = 1.0 / p;
+      r.fact = K;
+      for (int ax = 0; ax < 3; ax++) {
+        r.P[ax] = (a * A[ax] + b * Bc[ax]) * p_inv;
+        r.PA[ax] = r.P[ax] - A[ax];
+        r.PB[ax] = r.P[ax] - Bc[ax];
+      }
+      r.coef = B.c_gauss[m1 + (int64_t)B.ld * (i + (int64_t)B.n * ti)] *
+               B.c_gauss[m2 + (int64_t)B.ld * (k + (int64_t)B.n * tk)];
+      if (fold && m1 != m2) r.coef = 2.0 * r.coef;
+      out.push_back(r);
+    }
+  return out;
+}
+
+int pair_L(const BasisDev& B, int f1, int f2) {
+  int L = 0;
+  for (int ax = 0; ax < 3; ax++) {
+    const int a = B.npower[3 * f1 + ax] + (B.i_type[f1] == 2 ? 2 : 0);
+    const int b = B.npower[3 * f2 + ax] + (B.i_type[f2] == 2 ? 2 : 0);
+    L = std::max(L, a + b);
+  }
+  return L;
+}
+
+template <int L, int TC, int LK>
+double quartet_value(const BasisDev& B, int fi, int fk, int fj, int fl, bool fold) {
+  constexpr bool T2 = TC > 0;
+  constexpr int NO = T2 ? 4 : 1;
+  constexpr int QW = 3 * NO * (LK + 1);
+  const std::vector<PrimPair> bra = build_pairs(B, fi, fk, fold), ket = build_pairs(B, fj, fl, fold);
+  const QuartetShape S = quartet_shape<T2>(B, fi, fk, fj, fl);
+  std::vector<double> q(ket.size() * QW, 0.0);
+  for (size_t t = 0; t < ket.size(); t++) pair_polys<LK, T2, double>(S, 1, ket[t], &q[t * QW]);
+  const double* tab = boys_tables();
+  double acc = 0.0;
+  double Pn[3 * NO * (L + 1)] = {};
+  for (const PrimPair& P : bra) {
+    pair_polys<L, T2, double>(S, 0, P, Pn);
+    for (size_t t = 0; t < ket.size(); t++) {
+      const double v = prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
+      acc = std::fma(P.coef * ket[t].coef, v, acc);
+    }
+  }
+  return acc;
+}
+
+// the instance launch_eri_class (csrc/eri.cu) runs for (L, LK, tc)
+double dispatch(int L, int LK, int tc, const BasisDev& B, int fi, int fk, int fj, int fl, bool fold, int* bad) {
+#define Q(a, b, c) return quartet_value<a, b, c>(B, fi, fk, fj, fl, fold)
+  if (LK < L) {
+    if (LK == 1) {
+      if (L == 3 && tc == 0) Q(3, 0, 1);
+      if (L == 3 && tc == 1) Q(3, 1, 1);
+      if (L == 3 && tc == 2) Q(3, 2, 1);
+      if (L == 4 && tc == 0) Q(4, 0, 1);
+      if (L == 4 && tc == 1) Q(4, 1, 1);
+      if (L == 4 && tc == 2) Q(4, 2, 1);
+    } else if (LK == 2) {
+      if (L == 3 && tc == 0) Q(3, 0, 2);
+      if (L == 3 && tc == 1) Q(3, 1, 2);
+      if (L == 3 && tc == 2) Q(3, 2, 2);
+      if (L == 4 && tc == 0) Q(4, 0, 2);
+      if (L == 4 && tc == 1) Q(4, 1, 2);
+      if (L == 4 && tc == 2) Q(4, 2, 2);
+      if (L == 4 && tc == 3) Q(4, 3, 2);
+    }
+  } else if (tc == 0) {
+    if (L == 0) Q(0, 0, 0);
+    if (L == 1) Q(1, 0, 1);
+    if (L == 2) Q(2, 0, 2);
+    if (L == 3) Q(3, 0, 3);
+    if (L == 4) Q(4, 0, 4);
+  } else if (tc == 1) {
+    if (L <= 2) Q(2, 1, 2);
+    if (L == 3) Q(3, 1, 3);
+    if (L == 4) Q(4, 1, 4);
+  } else if (tc == 2) {
+    if (L <= 2) Q(2, 2, 2);
+    if (L == 3) Q(3, 2, 3);
+    if (L == 4) Q(4, 2, 4);
+  } else if (tc == 3) {
+    if (L <= 4) Q(4, 3, 4);
+  } else if (tc == 4) {
+    if (L <= 4) Q(4, 4, 4);
+  }
+#undef Q
+  *bad = 1;
+  return 0.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// mode 0: the device's instance choice (light-ket instances, lighter pair as the ket);
+// mode 1: full instances only (LK = L), no swap; mode 2: full instances, every quartet as (jl|ik).
+// fold: fold the same-fit pairs as the device does.  lk_out[q] = the ket bound used.
+int ss_host_eri(int n, int ld, const double* center, const int* npower, const int* nsto, const int* itype,
+                const int* ng, const double* cg, const double* gg, const double* gs, int64_t nint,
+                const int32_t* is, const int32_t* js, const int32_t* ks, const int32_t* ls, int mode, int fold,
+                double* out, int* lk_out) {
+  BasisDev B{n, ld, center, npower, nsto, itype, ng, cg, gg, gs};
+  int bad = 0;
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    const int Lb = pair_L(B, i, k), Lk = pair_L(B, j, l);
+    const int L = std::max(Lb, Lk);
+    const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
+    const int lmin = std::min(Lb, Lk);
+    const int v = (mode == 0 && L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    const bool swp = (v && Lk > Lb) || mode == 2;
+    if (swp) {
+      std::swap(i, j);
+      std::swap(k, l);
+    }
+    const int LK = v ? v : L;
+    lk_out[q] = LK;
+    out[q] = dispatch(L, LK, tc, B, i, k, j, l, fold != 0, &bad);
+  }
+  return bad;
+}
+
+}  // extern "C"
