@@ -133,9 +133,16 @@ int ss_write_bielec_ao(ss_ctx* c, const char* path) {
     ss_set_cuda_error(e, "cudaMallocHost", __FILE__, __LINE__);
     return SS_ERR_NOMEM;
   }
-  cudaEvent_t ev[2];
-  cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    if (ev[0]) cudaEventDestroy(ev[0]);
+    cudaFreeHost(h);
+    fclose(f);
+    ss_set_cuda_error(e, "cudaEventCreate", __FILE__, __LINE__);
+    return SS_ERR_CUDA;
+  }
   auto issue = [&](int64_t q0, int slot) {
     const int64_t n = std::min(chunk, c->nint - q0);
     double* hv = h + (size_t)slot * 2 * chunk;
