@@ -105,48 +105,158 @@ double quartet_value(const BasisDev& B, int fi, int fk, int fj, int fl, bool fol
   return acc;
 }
 
-// the instance launch_eri_class (csrc/eri.cu) runs for (L, LK, tc)
+// the instance launch_eri_class (csrc/eri.cu) runs for (L, LK, tc): SS_HOST_DISPATCH(F, args)
+// returns F<L, TC, LK>(args) for it (bad = 1 when there is none)
+#define SS_HOST_DISPATCH(F, ...)                                   \
+  do {                                                             \
+    if (LK < L) {                                                  \
+      if (LK == 1) {                                               \
+        if (L == 3 && tc == 0) return F<3, 0, 1>(__VA_ARGS__);     \
+        if (L == 3 && tc == 1) return F<3, 1, 1>(__VA_ARGS__);     \
+        if (L == 3 && tc == 2) return F<3, 2, 1>(__VA_ARGS__);     \
+        if (L == 4 && tc == 0) return F<4, 0, 1>(__VA_ARGS__);     \
+        if (L == 4 && tc == 1) return F<4, 1, 1>(__VA_ARGS__);     \
+        if (L == 4 && tc == 2) return F<4, 2, 1>(__VA_ARGS__);     \
+      } else if (LK == 2) {                                        \
+        if (L == 3 && tc == 0) return F<3, 0, 2>(__VA_ARGS__);     \
+        if (L == 3 && tc == 1) return F<3, 1, 2>(__VA_ARGS__);     \
+        if (L == 3 && tc == 2) return F<3, 2, 2>(__VA_ARGS__);     \
+        if (L == 4 && tc == 0) return F<4, 0, 2>(__VA_ARGS__);     \
+        if (L == 4 && tc == 1) return F<4, 1, 2>(__VA_ARGS__);     \
+        if (L == 4 && tc == 2) return F<4, 2, 2>(__VA_ARGS__);     \
+        if (L == 4 && tc == 3) return F<4, 3, 2>(__VA_ARGS__);     \
+      }                                                            \
+    } else if (tc == 0) {                                          \
+      if (L == 0) return F<0, 0, 0>(__VA_ARGS__);                  \
+      if (L == 1) return F<1, 0, 1>(__VA_ARGS__);                  \
+      if (L == 2) return F<2, 0, 2>(__VA_ARGS__);                  \
+      if (L == 3) return F<3, 0, 3>(__VA_ARGS__);                  \
+      if (L == 4) return F<4, 0, 4>(__VA_ARGS__);                  \
+    } else if (tc == 1) {                                          \
+      if (L <= 2) return F<2, 1, 2>(__VA_ARGS__);                  \
+      if (L == 3) return F<3, 1, 3>(__VA_ARGS__);                  \
+      if (L == 4) return F<4, 1, 4>(__VA_ARGS__);                  \
+    } else if (tc == 2) {                                          \
+      if (L <= 2) return F<2, 2, 2>(__VA_ARGS__);                  \
+      if (L == 3) return F<3, 2, 3>(__VA_ARGS__);                  \
+      if (L == 4) return F<4, 2, 4>(__VA_ARGS__);                  \
+    } else if (tc == 3) {                                          \
+      if (L <= 4) return F<4, 3, 4>(__VA_ARGS__);                  \
+    } else if (tc == 4) {                                          \
+      if (L <= 4) return F<4, 4, 4>(__VA_ARGS__);                  \
+    }                                                              \
+  } while (0)
+
 double dispatch(int L, int LK, int tc, const BasisDev& B, int fi, int fk, int fj, int fl, bool fold, int* bad) {
-#define Q(a, b, c) return quartet_value<a, b, c>(B, fi, fk, fj, fl, fold)
-  if (LK < L) {
-    if (LK == 1) {
-      if (L == 3 && tc == 0) Q(3, 0, 1);
-      if (L == 3 && tc == 1) Q(3, 1, 1);
-      if (L == 3 && tc == 2) Q(3, 2, 1);
-      if (L == 4 && tc == 0) Q(4, 0, 1);
-      if (L == 4 && tc == 1) Q(4, 1, 1);
-      if (L == 4 && tc == 2) Q(4, 2, 1);
-    } else if (LK == 2) {
-      if (L == 3 && tc == 0) Q(3, 0, 2);
-      if (L == 3 && tc == 1) Q(3, 1, 2);
-      if (L == 3 && tc == 2) Q(3, 2, 2);
-      if (L == 4 && tc == 0) Q(4, 0, 2);
-      if (L == 4 && tc == 1) Q(4, 1, 2);
-      if (L == 4 && tc == 2) Q(4, 2, 2);
-      if (L == 4 && tc == 3) Q(4, 3, 2);
-    }
-  } else if (tc == 0) {
-    if (L == 0) Q(0, 0, 0);
-    if (L == 1) Q(1, 0, 1);
-    if (L == 2) Q(2, 0, 2);
-    if (L == 3) Q(3, 0, 3);
-    if (L == 4) Q(4, 0, 4);
-  } else if (tc == 1) {
-    if (L <= 2) Q(2, 1, 2);
-    if (L == 3) Q(3, 1, 3);
-    if (L == 4) Q(4, 1, 4);
-  } else if (tc == 2) {
-    if (L <= 2) Q(2, 2, 2);
-    if (L == 3) Q(3, 2, 3);
-    if (L == 4) Q(4, 2, 4);
-  } else if (tc == 3) {
-    if (L <= 4) Q(4, 3, 4);
-  } else if (tc == 4) {
-    if (L <= 4) Q(4, 4, 4);
-  }
-#undef Q
+  SS_HOST_DISPATCH(quartet_value, B, fi, fk, fj, fl, fold);
   *bad = 1;
   return 0.0;
+}
+
+// Schwarz factors S_P = sqrt(c_P^2 (PP|PP)) of a pair list, as the kernel's self mode computes
+// them (the instance of the quartet (ik|ik))
+template <int L, int TC, int LK>
+std::vector<double> self_factors(const BasisDev& B, int i, int k, const std::vector<PrimPair>& pairs) {
+  constexpr bool T2 = TC > 0;
+  constexpr int NO = T2 ? 4 : 1;
+  const QuartetShape S = quartet_shape<T2>(B, i, k, i, k);
+  const double* tab = boys_tables();
+  std::vector<double> out(pairs.size());
+  double Pn[3 * NO * (L + 1)] = {}, Qn[3 * NO * (LK + 1)] = {};
+  for (size_t t = 0; t < pairs.size(); t++) {
+    pair_polys<L, T2, double>(S, 0, pairs[t], Pn);
+    pair_polys<LK, T2, double>(S, 1, pairs[t], Qn);
+    const double v = prim_quartet<L, TC, double, LK>(S, view64(pairs[t]), Pn, view64(pairs[t]), Qn, tab);
+    out[t] = std::sqrt(std::fmax((pairs[t].coef * pairs[t].coef) * v, 0.0));
+  }
+  return out;
+}
+
+std::vector<double> schwarz(const BasisDev& B, int i, int k, const std::vector<PrimPair>& pairs, int* bad) {
+  const int L = pair_L(B, i, k), LK = L;
+  const int tc = 2 * ((B.i_type[i] == 2) + (B.i_type[k] == 2));
+  SS_HOST_DISPATCH(self_factors, B, i, k, pairs);
+  *bad = 1;
+  return {};
+}
+
+PrimPairF to_f32(const PrimPair& a) {  // prim_pair_to_f32 (csrc/eri.cu)
+  PrimPairF f{};
+  f.p = (float)a.p;
+  f.p_inv = (float)a.p_inv;
+  f.fc = (float)(a.fact * a.coef);
+  for (int ax = 0; ax < 3; ax++) {
+    f.P[ax] = (float)a.P[ax];
+    f.PA[ax] = (float)a.PA[ax];
+    f.PB[ax] = (float)a.PB[ax];
+  }
+  return f;
+}
+
+struct Fp32Err {
+  double all = 0.0, tier = 0.0;  // max |v32 - v64| / (S_P S_Q) over primitive quartets
+  int64_t n_all = 0, n_tier = 0;
+  // over quartets: max |sum_tier (v32 - v64)| / sqrt((ik|ik)(jl|jl)) (what the tier changes in
+  // the ERI) and max sum_tier |v32 - v64| / sqrt((ik|ik)(jl|jl)) (no cancellation between terms)
+  double q_signed = 0.0, q_abs = 0.0;
+};
+
+// the FP32 evaluation of every primitive quartet of one quartet against the FP64 one, as the
+// kernel's tiers form them (bra polynomials in FP32 from the FP32 pair copy, ket polynomials
+// rounded from FP64, K_AB c folded into the FP32 factor)
+template <int L, int TC, int LK>
+int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, Fp32Err* e) {
+  constexpr bool T2 = TC > 0;
+  constexpr int NO = T2 ? 4 : 1;
+  constexpr int QW = 3 * NO * (LK + 1);
+  const std::vector<PrimPair> bra = build_pairs(B, fi, fk, true), ket = build_pairs(B, fj, fl, true);
+  int bad = 0;
+  const std::vector<double> Sb = schwarz(B, fi, fk, bra, &bad), Sk = schwarz(B, fj, fl, ket, &bad);
+  if (bad) return 1;
+  const QuartetShape S = quartet_shape<T2>(B, fi, fk, fj, fl);
+  std::vector<double> q(ket.size() * QW, 0.0);
+  std::vector<float> qf(ket.size() * QW, 0.f);
+  for (size_t t = 0; t < ket.size(); t++) {
+    pair_polys<LK, T2, double>(S, 1, ket[t], &q[t * QW]);
+    for (int w = 0; w < QW; w++) qf[t * QW + w] = (float)q[t * QW + w];
+  }
+  const double* tab = boys_tables();
+  double Pn[3 * NO * (L + 1)] = {};
+  float Pf[3 * NO * (L + 1)] = {};
+  double s_signed = 0.0, s_abs = 0.0;
+  for (size_t b = 0; b < bra.size(); b++) {
+    const PrimPair& P = bra[b];
+    const PrimPairF P32 = to_f32(P);
+    pair_polys<L, T2, double>(S, 0, P, Pn);
+    pair_polys<L, T2, float>(S, 0, P32, Pf);
+    for (size_t t = 0; t < ket.size(); t++) {
+      const double v64 =
+          (P.coef * ket[t].coef) * prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
+      const float v32 =
+          prim_quartet<L, TC, float, LK>(S, view32(P32), Pf, view32(to_f32(ket[t])), &qf[t * QW], boys32_tab);
+      const double bound = Sb[b] * Sk[t];
+      if (!(bound > 0.0)) continue;
+      const double r = std::fabs((double)v32 - v64) / bound;
+      e->all = std::max(e->all, r);
+      e->n_all++;
+      if (bound < PRIM_FP32_EPS * sch) {
+        e->tier = std::max(e->tier, r);
+        e->n_tier++;
+        s_signed += (double)v32 - v64;
+        s_abs += std::fabs((double)v32 - v64);
+      }
+    }
+  }
+  if (sch > 0.0) {
+    e->q_signed = std::max(e->q_signed, std::fabs(s_signed) / sch);
+    e->q_abs = std::max(e->q_abs, s_abs / sch);
+  }
+  return 0;
+}
+
+int dispatch_fp32(int L, int LK, int tc, const BasisDev& B, int fi, int fk, int fj, int fl, double sch, Fp32Err* e) {
+  SS_HOST_DISPATCH(fp32_errors, B, fi, fk, fj, fl, sch, e);
+  return 1;
 }
 
 }  // namespace
@@ -179,6 +289,39 @@ int ss_host_eri(int n, int ld, const double* center, const int* npower, const in
     out[q] = dispatch(L, LK, tc, B, i, k, j, l, fold != 0, &bad);
   }
   return bad;
+}
+
+// Largest |FP32 - FP64| of a primitive quartet relative to its Schwarz bound S_P S_Q, over all
+// primitive quartets of the listed quartets and over those below the FP32-tier threshold
+// (S_P S_Q < PRIM_FP32_EPS sqrt((ik|ik)(jl|jl)), pre = the Schwarz diagonal, n x n column-major).
+int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, const int* nsto, const int* itype,
+                       const int* ng, const double* cg, const double* gg, const double* gs, int64_t nint,
+                       const int32_t* is, const int32_t* js, const int32_t* ks, const int32_t* ls,
+                       const double* pre,
+                       double* out /* max_all, max_tier, n_all, n_tier, q_signed, q_abs */) {
+  BasisDev B{n, ld, center, npower, nsto, itype, ng, cg, gg, gs};
+  Fp32Err e;
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    const int Lb = pair_L(B, i, k), Lk = pair_L(B, j, l);
+    const int L = std::max(Lb, Lk);
+    const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
+    const int lmin = std::min(Lb, Lk);
+    const int v = (L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    const double sch = std::sqrt(pre[i + (int64_t)n * k] * pre[j + (int64_t)n * l]);
+    if (v && Lk > Lb) {
+      std::swap(i, j);
+      std::swap(k, l);
+    }
+    if (dispatch_fp32(L, v ? v : L, tc, B, i, k, j, l, sch, &e)) return 1;
+  }
+  out[0] = e.all;
+  out[1] = e.tier;
+  out[2] = (double)e.n_all;
+  out[3] = (double)e.n_tier;
+  out[4] = e.q_signed;
+  out[5] = e.q_abs;
+  return 0;
 }
 
 }  // extern "C"

@@ -97,3 +97,47 @@ def test_folding_is_exact(lib):
     u, _ = _host_eri(lib, b, q, fold=0)
     big = np.abs(u) > 1e-12 * np.abs(u).max()
     assert np.max(np.abs(f[big] - u[big]) / np.abs(u[big])) < 1e-13
+
+
+def _fp32_error(lib, b, q, pre):
+    arrs = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
+            np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
+            np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
+            np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
+    qq = [np.ascontiguousarray(x, np.int32) for x in q]
+    out = np.zeros(6)
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
+    lib.ss_host_fp32_error.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
+                                       i32p, i32p, i32p, i32p, f64p, f64p]
+    assert lib.ss_host_fp32_error(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq,
+                                  np.ascontiguousarray(pre, np.float64), out) == 0
+    return {"n_tier": int(out[3]), "signed": out[4], "abs": out[5]}
+
+
+def test_fp32_tier_error_is_negligible(lib, h2o26):
+    """The FP32 tier (primitive quartets below 1e-13 of the Schwarz bound sqrt((ik|ik)(jl|jl)),
+    evaluated as the kernel does: FP32 bra polynomials from the FP32 pair copies, ket polynomials
+    rounded from FP64, K_AB c folded into the FP32 factor) changes each ERI by far less than the
+    1e-12 gate: the sum of |FP32 - FP64| over a quartet's tier stays below 1e-15 of its Schwarz
+    bound.  (A single primitive quartet can be off by its whole bound when its FP32 prefactor
+    underflows, but such terms are ~1e-40 in absolute size.)  Every quartet of the 26-function
+    basis at 3-Gaussian fits, and 10 quartets at the production 20-Gaussian fits."""
+    from oracle import binding as O
+    b, q, pre, ref = h2o26
+    e = _fp32_error(lib, b, q, pre)
+    assert e["n_tier"] > 0 and e["abs"] < 1e-15
+    b20 = configs.h2o_26(ng0=20)
+    q20 = np.array(basis.build_mapping(b20.n))
+    sel = np.random.default_rng(11).choice(q20.shape[1], 10, replace=False)
+    qs = q20[:, sel]
+    # the Schwarz diagonal entries these quartets need, from the oracle
+    pairs = sorted({(int(i), int(k)) for i, k in zip(qs[0], qs[2])} | {(int(j), int(l)) for j, l in zip(qs[1], qs[3])})
+    pq = [np.array([p[0] for p in pairs]), np.array([p[0] for p in pairs]),
+          np.array([p[1] for p in pairs]), np.array([p[1] for p in pairs])]
+    diag, _ = O.gauss_eri(O.OracleBasis(b20), pq)
+    pre20 = np.zeros((b20.n, b20.n))
+    for (i, k), v in zip(pairs, diag):
+        pre20[i - 1, k - 1] = pre20[k - 1, i - 1] = v
+    e20 = _fp32_error(lib, b20, [qs[r] for r in range(4)], pre20.reshape(-1, order="F"))
+    assert e20["n_tier"] > 100000 and e20["abs"] < 1e-15
