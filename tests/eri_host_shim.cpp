@@ -205,7 +205,7 @@ struct Fp32Err {
 // kernel's tiers form them (bra polynomials in FP32 from the FP32 pair copy, ket polynomials
 // rounded from FP64, K_AB c folded into the FP32 factor)
 template <int L, int TC, int LK>
-int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, Fp32Err* e) {
+int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, double eps32, Fp32Err* e) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;
   constexpr int QW = 3 * NO * (LK + 1);
@@ -239,7 +239,7 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, F
       const double r = std::fabs((double)v32 - v64) / bound;
       e->all = std::max(e->all, r);
       e->n_all++;
-      if (bound < PRIM_FP32_EPS * sch) {
+      if (bound < eps32 * sch) {
         e->tier = std::max(e->tier, r);
         e->n_tier++;
         s_signed += (double)v32 - v64;
@@ -254,8 +254,9 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, F
   return 0;
 }
 
-int dispatch_fp32(int L, int LK, int tc, const BasisDev& B, int fi, int fk, int fj, int fl, double sch, Fp32Err* e) {
-  SS_HOST_DISPATCH(fp32_errors, B, fi, fk, fj, fl, sch, e);
+int dispatch_fp32(int L, int LK, int tc, const BasisDev& B, int fi, int fk, int fj, int fl, double sch,
+                  double eps32, Fp32Err* e) {
+  SS_HOST_DISPATCH(fp32_errors, B, fi, fk, fj, fl, sch, eps32, e);
   return 1;
 }
 
@@ -293,11 +294,12 @@ int ss_host_eri(int n, int ld, const double* center, const int* npower, const in
 
 // Largest |FP32 - FP64| of a primitive quartet relative to its Schwarz bound S_P S_Q, over all
 // primitive quartets of the listed quartets and over those below the FP32-tier threshold
-// (S_P S_Q < PRIM_FP32_EPS sqrt((ik|ik)(jl|jl)), pre = the Schwarz diagonal, n x n column-major).
+// (S_P S_Q < eps32 sqrt((ik|ik)(jl|jl)); the kernel's eps32 is PRIM_FP32_EPS; pre = the Schwarz
+// diagonal, n x n column-major).
 int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, const int* nsto, const int* itype,
                        const int* ng, const double* cg, const double* gg, const double* gs, int64_t nint,
                        const int32_t* is, const int32_t* js, const int32_t* ks, const int32_t* ls,
-                       const double* pre,
+                       const double* pre, double eps32,
                        double* out /* max_all, max_tier, n_all, n_tier, q_signed, q_abs */) {
   BasisDev B{n, ld, center, npower, nsto, itype, ng, cg, gg, gs};
   Fp32Err e;
@@ -313,7 +315,7 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
       std::swap(i, j);
       std::swap(k, l);
     }
-    if (dispatch_fp32(L, v ? v : L, tc, B, i, k, j, l, sch, &e)) return 1;
+    if (dispatch_fp32(L, v ? v : L, tc, B, i, k, j, l, sch, eps32, &e)) return 1;
   }
   out[0] = e.all;
   out[1] = e.tier;

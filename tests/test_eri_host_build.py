@@ -17,6 +17,7 @@ import pytest
 from slater_stoch_gb300 import basis, configs
 
 HERE = Path(__file__).resolve().parent
+PRIM_FP32_EPS = 1e-13  # the kernel's threshold of the FP32 tier (csrc/ss_common.cuh)
 CSRC = HERE.parent / "slater_stoch_gb300" / "csrc"
 
 
@@ -109,9 +110,9 @@ def _fp32_error(lib, b, q, pre):
     f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
     lib.ss_host_fp32_error.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
-                                       i32p, i32p, i32p, i32p, f64p, f64p]
+                                       i32p, i32p, i32p, i32p, f64p, C.c_double, f64p]
     assert lib.ss_host_fp32_error(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq,
-                                  np.ascontiguousarray(pre, np.float64), out) == 0
+                                  np.ascontiguousarray(pre, np.float64), PRIM_FP32_EPS, out) == 0
     return {"n_tier": int(out[3]), "signed": out[4], "abs": out[5]}
 
 
@@ -141,3 +142,11 @@ def test_fp32_tier_error_is_negligible(lib, h2o26):
         pre20[i - 1, k - 1] = pre20[k - 1, i - 1] = v
     e20 = _fp32_error(lib, b20, [qs[r] for r in range(4)], pre20.reshape(-1, order="F"))
     assert e20["n_tier"] > 100000 and e20["abs"] < 1e-15
+
+
+def test_threshold_matches_the_kernel():
+    """The FP32-tier threshold used above is the kernel's (csrc/ss_common.cuh)."""
+    import re
+    src = (CSRC / "ss_common.cuh").read_text()
+    m = re.search(r"constexpr double PRIM_FP32_EPS = ([0-9.eE+-]+);", src)
+    assert m and float(m.group(1)) == PRIM_FP32_EPS
