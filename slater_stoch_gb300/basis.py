@@ -168,6 +168,8 @@ def build_basis(mol: Molecule, basis: Dict[int, List[Tuple[str, float]]],
         for orb, zeta in basis.get(Z, []):
             if orb not in ORBITALS:
                 raise ValueError(f"orbital {orb} is not supported by the fit builder")
+            if not (zeta > 0.0 and np.isfinite(zeta)):
+                raise ValueError(f"{sym} {orb}: Slater exponent {zeta} must be positive and finite")
             nsto, itype, comps, extra = ORBITALS[orb]
             ng = fit.ng0
             if extra == "2p":

@@ -148,3 +148,19 @@ def test_library_bielec_ao_writer_matches_fortran_format(tmp_path):
     api.write_bielec_ao_arrays(tmp_path / "lib.txt", q, v, s)
     output.write_bielec_ao(tmp_path / "py.txt", q, v, s)
     assert (tmp_path / "lib.txt").read_bytes() == (tmp_path / "py.txt").read_bytes()
+
+
+def test_corrupt_inputs_rejected(tmp_path):
+    """Malformed inputs stop with an error instead of reaching the device: a non-numeric or
+    non-positive Slater exponent, an orbital the fit builder does not know, a geometry file with
+    fewer atoms than it announces."""
+    mol = basis.molecule_bohr(["O"], [[0.0, 0.0, 0.0]])
+    (tmp_path / "bad_zeta").write_text("O 1S seven\n")
+    with pytest.raises(ValueError):
+        basis.read_basis(tmp_path / "bad_zeta")
+    for bad in ({8: [("1S", -1.0)]}, {8: [("1S", float("nan"))]}, {8: [("6H", 1.0)]}):
+        with pytest.raises(ValueError):
+            basis.build_basis(mol, bad, basis.FitParams(ng0=4))
+    (tmp_path / "short.xyz").write_text("3\nWater\nO 0. 0. 0.\nH 0.0 0.75 0.58\n")
+    with pytest.raises(ValueError):
+        basis.read_geometry(tmp_path / "short.xyz")

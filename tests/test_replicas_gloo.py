@@ -52,3 +52,36 @@ def test_two_gloo_ranks_agree_on_the_slowest_time():
 def test_single_rank_is_identity():
     assert max_over_ranks(5.0, 1) == 5.0
     assert whole_job_throughput(100, 1, 2.0) == 50.0
+
+
+def _lost_rank(rank, world, port, out):
+    import datetime
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=10))
+    if rank == 1:
+        os._exit(0)  # the rank leaves between steps, before the timing reduction
+    try:
+        max_over_ranks(1.0, world, dist, "cpu")
+        out[rank] = "no error"
+    except Exception as e:  # the lost peer surfaces as an error, not a hang
+        out[rank] = "error: " + type(e).__name__
+
+
+def test_lost_rank_is_reported():
+    """A rank that exits between steps: the surviving rank's next collective ends with an error
+    (peer closed or the 10 s process-group timeout) instead of hanging."""
+    world = 2
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as m:
+        out = m.dict()
+        procs = [ctx.Process(target=_lost_rank, args=(r, world, port, out)) for r in range(world)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(timeout=120)
+        assert all(p.exitcode is not None for p in procs)
+        res = dict(out)
+    assert res.get(0, "").startswith("error")
