@@ -30,7 +30,8 @@ class OrcBasis(C.Structure):
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build()
+        # SS_ORACLE_LIB: an alternative build of the same source (the sanitizer test's)
+        path = os.environ.get("SS_ORACLE_LIB") or _build.build()
         L = C.CDLL(str(path))
         L.orc_rint_sum.restype = C.c_double
         L.orc_rint_sum.argtypes = [C.c_int, C.c_double, f64p]
