@@ -62,3 +62,20 @@ int ss_host_admission_run(int njobs, const long long* bytes, const int* abandon,
 }
 
 }  // extern "C"
+
+#ifdef SS_ADMISSION_MAIN
+// standalone run of the scenarios for the thread-sanitizer build: exit status 0 when every
+// scenario drained its queue
+int main() {
+  const long long b6[6] = {100, 100, 100, 100, 100, 100};
+  const int none[6] = {0, 0, 0, 0, 0, 0}, ab[6] = {0, 1, 0, 0, 0, 0};
+  int order[6], refused[6], pr, spr;
+  long long pb, spb;
+  int rc = 0;
+  rc |= ss_host_admission_run(6, b6, none, 0, 2, 5, order, refused, &pr, &pb, &spr, &spb);
+  rc |= ss_host_admission_run(6, b6, none, 250, 0, 5, order, refused, &pr, &pb, &spr, &spb);
+  rc |= ss_host_admission_run(6, b6, ab, 0, 1, 5, order, refused, &pr, &pb, &spr, &spb);
+  rc |= ss_host_admission_run(6, b6, none, 0, 0, 5, order, refused, &pr, &pb, &spr, &spb);
+  return rc;
+}
+#endif

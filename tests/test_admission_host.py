@@ -69,3 +69,21 @@ def test_abandoned_ticket_does_not_block_the_queue(lib):
 def test_unlimited_runs_all_at_once(lib):
     order, refused, pr, pb, spr, spb = _run(lib, [100] * 4, sleep_ms=1000)
     assert spr >= 2 and spb == 100 * spr  # jobs overlap when nothing limits them
+
+
+def test_admission_under_thread_sanitizer(tmp_path):
+    """The admission scenarios built as a standalone program with ThreadSanitizer: no data race
+    is reported and every queue drains."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "adm_tsan"
+    r = subprocess.run([gxx, "-O1", "-g", "-std=c++17", "-pthread", "-fsanitize=thread", "-DSS_ADMISSION_MAIN",
+                        f"-I{CSRC}", str(HERE / "admission_host_shim.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("ThreadSanitizer build not available: " + r.stderr[-200:])
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300,
+                         env={"TSAN_OPTIONS": "halt_on_error=1"})
+    assert "ThreadSanitizer" not in run.stderr, run.stderr[-3000:]
+    assert run.returncode == 0
