@@ -199,6 +199,9 @@ struct Fp32Err {
   // over quartets: max |sum_tier (v32 - v64)| / sqrt((ik|ik)(jl|jl)) (what the tier changes in
   // the ERI) and max sum_tier |v32 - v64| / sqrt((ik|ik)(jl|jl)) (no cancellation between terms)
   double q_signed = 0.0, q_abs = 0.0;
+  // max over quartets of |FP32 running sums - exact sum of the FP32 terms| / Schwarz bound, the
+  // tier's items dealt to 128 threads in contiguous runs (bra-major), each summed in float
+  double q_acc = 0.0;
 };
 
 // the FP32 evaluation of every primitive quartet of one quartet against the FP64 one, as the
@@ -224,6 +227,7 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, d
   double Pn[3 * NO * (L + 1)] = {};
   float Pf[3 * NO * (L + 1)] = {};
   double s_signed = 0.0, s_abs = 0.0;
+  std::vector<float> tier_terms;
   for (size_t b = 0; b < bra.size(); b++) {
     const PrimPair& P = bra[b];
     const PrimPairF P32 = to_f32(P);
@@ -244,12 +248,24 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, d
         e->n_tier++;
         s_signed += (double)v32 - v64;
         s_abs += std::fabs((double)v32 - v64);
+        tier_terms.push_back(v32);
       }
     }
   }
   if (sch > 0.0) {
     e->q_signed = std::max(e->q_signed, std::fabs(s_signed) / sch);
     e->q_abs = std::max(e->q_abs, s_abs / sch);
+    const size_t nt = tier_terms.size(), per = (nt + 127) / 128;
+    double dev = 0.0, exact = 0.0;
+    for (size_t t0 = 0; t0 < nt; t0 += per) {
+      float acc32 = 0.f;
+      for (size_t t = t0; t < std::min(nt, t0 + per); t++) {
+        acc32 += tier_terms[t];
+        exact += (double)tier_terms[t];
+      }
+      dev += (double)acc32;
+    }
+    e->q_acc = std::max(e->q_acc, std::fabs(dev - exact) / sch);
   }
   return 0;
 }
@@ -300,7 +316,7 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
                        const int* ng, const double* cg, const double* gg, const double* gs, int64_t nint,
                        const int32_t* is, const int32_t* js, const int32_t* ks, const int32_t* ls,
                        const double* pre, double eps32,
-                       double* out /* max_all, max_tier, n_all, n_tier, q_signed, q_abs */) {
+                       double* out /* max_all, max_tier, n_all, n_tier, q_signed, q_abs, q_acc */) {
   BasisDev B{n, ld, center, npower, nsto, itype, ng, cg, gg, gs};
   Fp32Err e;
   for (int64_t q = 0; q < nint; q++) {
@@ -323,6 +339,7 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
   out[3] = (double)e.n_tier;
   out[4] = e.q_signed;
   out[5] = e.q_abs;
+  out[6] = e.q_acc;
   return 0;
 }
 

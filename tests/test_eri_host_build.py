@@ -106,14 +106,14 @@ def _fp32_error(lib, b, q, pre):
             np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
             np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
     qq = [np.ascontiguousarray(x, np.int32) for x in q]
-    out = np.zeros(6)
+    out = np.zeros(7)
     f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
     i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
     lib.ss_host_fp32_error.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
                                        i32p, i32p, i32p, i32p, f64p, C.c_double, f64p]
     assert lib.ss_host_fp32_error(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq,
                                   np.ascontiguousarray(pre, np.float64), PRIM_FP32_EPS, out) == 0
-    return {"n_tier": int(out[3]), "signed": out[4], "abs": out[5]}
+    return {"n_tier": int(out[3]), "signed": out[4], "abs": out[5], "acc": out[6]}
 
 
 def test_fp32_tier_error_is_negligible(lib, h2o26):
@@ -142,6 +142,7 @@ def test_fp32_tier_error_is_negligible(lib, h2o26):
         pre20[i - 1, k - 1] = pre20[k - 1, i - 1] = v
     e20 = _fp32_error(lib, b20, [qs[r] for r in range(4)], pre20.reshape(-1, order="F"))
     assert e20["n_tier"] > 100000 and e20["abs"] < 1e-15
+    assert e20["acc"] < 1e-15  # the per-thread FP32 running sums
 
 
 def test_threshold_matches_the_kernel():
