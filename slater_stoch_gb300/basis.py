@@ -239,6 +239,18 @@ def build_mapping(n: int) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarra
             np.ascontiguousarray(a[:, 2]), np.ascontiguousarray(a[:, 3]))
 
 
+def count_multi_center(b: "Basis", quartets) -> Dict[int, int]:
+    """Number of quartets on 1, 2, 3 and 4 distinct nuclei (count_multi_center_integrals,
+    src/count_multi_center_integrals.F90:1-31, with compare_nuclei's ndiff = the number of
+    distinct nuclei of (i, j, k, l))."""
+    nuc = np.asarray(b.nucleus)
+    q = [np.asarray(x) - 1 for x in quartets]
+    stacked = np.stack([nuc[q[0]], nuc[q[1]], nuc[q[2]], nuc[q[3]]], axis=1)
+    stacked.sort(axis=1)
+    ndiff = 1 + (np.diff(stacked, axis=1) != 0).sum(axis=1)
+    return {d: int((ndiff == d).sum()) for d in (1, 2, 3, 4)}
+
+
 def read_j_in(path: str | Path) -> dict:
     """Positional input of two_e_slater (src/two_e_slater.F90:106-154)."""
     L = Path(path).read_text().splitlines()

@@ -164,3 +164,15 @@ def test_corrupt_inputs_rejected(tmp_path):
     (tmp_path / "short.xyz").write_text("3\nWater\nO 0. 0. 0.\nH 0.0 0.75 0.58\n")
     with pytest.raises(ValueError):
         basis.read_geometry(tmp_path / "short.xyz")
+
+
+def test_multi_center_counts():
+    """count_multi_center_integrals: the 26-function H2O list splits into 1-, 2-, 3- and
+    4-centre quartets that add up to nint; the one-centre count is the exact one-centre path's."""
+    from oracle import binding as O
+    b = configs.h2o_26(ng0=3)
+    q = basis.build_mapping(b.n)
+    c = basis.count_multi_center(b, q)
+    assert sum(c.values()) == len(q[0]) and c[4] == 0  # three atoms
+    _, mask = O.monocenter(O.OracleBasis(b), q)
+    assert c[1] == int(mask.sum()) == 9556
