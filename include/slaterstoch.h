@@ -122,6 +122,10 @@ int ss_one_e(ss_ctx* ctx, double* S, double* V, double* K);
 int ss_write_bielec_ao(ss_ctx* ctx, const char* path);
 int ss_write_bielec_ao_arrays(const char* path, int64_t nint, const int32_t* is, const int32_t* js,
                               const int32_t* ks, const int32_t* ls, const double* eri, const double* sigma);
+/* One matrix of ss_one_e (n x n column-major, [i,k]) in one_e_slater's text format
+ * (src/one_e_slater.F90:125-135: '(2(I5,X),D22.15)' i,k,M(i,k), i outer): the files
+ * overlap_ao_ex, nuclear_ao_ex and kinetic_ao_ex of the reference. */
+int ss_write_one_e_matrix(const char* path, int n, const double* m);
 
 /* Asynchronous job API (the reference runs one job per process and has none; these queue the
  * job of ss_two_e_job for a serving caller).  ss_job_submit copies the context's basis and

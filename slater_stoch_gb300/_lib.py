@@ -45,6 +45,7 @@ SIGNATURES = {
                                 C.c_double, C.c_void_p]),
     "ss_job_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "ss_job_result": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "ss_write_one_e_matrix": (C.c_int, [C.c_char_p, C.c_int, f64p]),
     "ss_job_limits": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
     "ss_job_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ss_job_footprint": (C.c_size_t, [C.c_int64]),

@@ -272,6 +272,17 @@ class Context:
         return ev, vec.T
 
 
+def write_one_e_ao(directory, S, V, K):
+    """one_e_slater's text outputs overlap_ao_ex, nuclear_ao_ex, kinetic_ao_ex (n x n, [i, k]),
+    written by the library."""
+    from pathlib import Path
+    L = _lib.load()
+    for name, M in (("overlap_ao_ex", S), ("nuclear_ao_ex", V), ("kinetic_ao_ex", K)):
+        M = np.asarray(M, dtype=np.float64)
+        flat = np.ascontiguousarray(M.reshape(-1, order="F"))
+        _lib.check(L.ss_write_one_e_matrix(str(Path(directory) / name).encode(), int(M.shape[0]), flat))
+
+
 def write_bielec_ao_arrays(path, quartets, eri, sigma=None):
     """bielec_ao text file of caller arrays, written by the library (no device needed)."""
     L = _lib.load()

@@ -102,6 +102,40 @@ int ss_write_bielec_ao_arrays(const char* path, int64_t nint, const int32_t* is,
   return rc;
 }
 
+// one-electron matrix file of one_e_slater (src/one_e_slater.F90:125-135):
+// write(u,'(2(I5,X),D22.15)') i,k,M(i,k) for i = 1..n (outer), k = 1..n
+int ss_write_one_e_matrix(const char* path, int n, const double* m) {
+  if (!path || n < 0 || (n > 0 && !m)) {
+    ss_set_error_msg("ss_write_one_e_matrix: bad arguments");
+    return SS_ERR_ARG;
+  }
+  FILE* f = fopen(path, "w");
+  if (!f) {
+    ss_set_error_msg("one-electron output: cannot open %s", path);
+    return SS_ERR_ARG;
+  }
+  std::vector<char> buf((size_t)std::max(n, 1) * 64);
+  int rc = SS_OK;
+  for (int i = 0; i < n && !rc; i++) {
+    size_t pos = 0;
+    for (int k = 0; k < n; k++) {
+      int nc = snprintf(buf.data() + pos, 32, "%5d %5d ", i + 1, k + 1);
+      fortran_d22_15(m[i + (size_t)n * k], buf.data() + pos + nc);
+      buf[pos + nc + 22] = '\n';
+      pos += (size_t)nc + 23;
+    }
+    if (fwrite(buf.data(), 1, pos, f) != pos) {
+      ss_set_error_msg("one-electron output: write failed");
+      rc = SS_ERR_STATE;
+    }
+  }
+  if (fclose(f) != 0 && !rc) {
+    ss_set_error_msg("one-electron output: close failed");
+    rc = SS_ERR_STATE;
+  }
+  return rc;
+}
+
 int ss_write_bielec_ao(ss_ctx* c, const char* path) {
   if (!c || !path) {
     ss_set_error_msg("ss_write_bielec_ao: null argument");

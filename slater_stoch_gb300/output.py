@@ -47,6 +47,16 @@ def write_bielec_ao(path, quartets, values, sigma) -> None:
                     f"{fortran_d(values[t])}{fortran_d(sigma[t])}\n")
 
 
+def write_one_e_matrix(path, M) -> None:
+    """one_e_slater's '(2(I5,X),D22.15)' i,k,M(i,k) records, i outer (src/one_e_slater.F90:125-135)."""
+    M = np.asarray(M)
+    n = M.shape[0]
+    with open(path, "w") as f:
+        for i in range(n):
+            for k in range(n):
+                f.write(f"{i + 1:5d} {k + 1:5d} {fortran_d(M[i, k])}\n")
+
+
 def read_bielec_ao(path) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
     idx, val, err = [], [], []
     for line in Path(path).read_text().splitlines():

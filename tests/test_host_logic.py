@@ -176,3 +176,17 @@ def test_multi_center_counts():
     assert sum(c.values()) == len(q[0]) and c[4] == 0  # three atoms
     _, mask = O.monocenter(O.OracleBasis(b), q)
     assert c[1] == int(mask.sum()) == 9556
+
+
+def test_library_one_e_writer_matches_fortran_format(tmp_path):
+    """The library's one-electron matrix files (overlap_ao_ex, nuclear_ao_ex, kinetic_ao_ex of
+    one_e_slater) are byte-identical to the '(2(I5,X),D22.15)' records written by output.py."""
+    from slater_stoch_gb300 import api, output
+    rng = np.random.default_rng(5)
+    n = 9
+    mats = [rng.standard_normal((n, n)) * 10.0 ** rng.integers(-110, 3, (n, n)) for _ in range(3)]
+    mats[0][0, 0] = 0.0
+    api.write_one_e_ao(tmp_path, *mats)
+    for name, M in zip(("overlap_ao_ex", "nuclear_ao_ex", "kinetic_ao_ex"), mats):
+        output.write_one_e_matrix(tmp_path / (name + ".py"), M)
+        assert (tmp_path / name).read_bytes() == (tmp_path / (name + ".py")).read_bytes()
