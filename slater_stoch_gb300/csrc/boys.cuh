@@ -79,7 +79,8 @@ SS_HD double exp_neg(double x, const double* e2) {
   q = fma(r, q, 1.0);
   const double tj = e2[k & 31];
   const double y = fma(tj, r * q, tj);
-  return from_bits(bits_of(y) + ((int64_t)(k >> 5) << 52));
+  // add k >> 5 (may be negative) to the exponent field; the shift is done on the unsigned bits
+  return from_bits((int64_t)((uint64_t)bits_of(y) + ((uint64_t)(int64_t)(k >> 5) << 52)));
 }
 
 // F_0(T) for 1 <= T <= 36 from the grid Taylor table (rows of BOYS_HI_J coefficients)

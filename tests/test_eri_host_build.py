@@ -151,3 +151,51 @@ def test_threshold_matches_the_kernel():
     src = (CSRC / "ss_common.cuh").read_text()
     m = re.search(r"constexpr double PRIM_FP32_EPS = ([0-9.eE+-]+);", src)
     assert m and float(m.group(1)) == PRIM_FP32_EPS
+
+
+SAN_SCRIPT = r"""
+import sys, ctypes as C, numpy as np
+sys.path.insert(0, sys.argv[1])
+from slater_stoch_gb300 import basis, configs
+L = C.CDLL(sys.argv[2])
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C"); i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
+L.ss_host_eri.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
+                          i32p, i32p, i32p, i32p, C.c_int, C.c_int, f64p, i32p]
+b = configs.h2o_26(ng0=2); q = basis.build_mapping(b.n)
+arrs = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
+        np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
+        np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
+        np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
+qq = [np.ascontiguousarray(x, np.int32) for x in q]
+for mode in (0, 1, 2):
+    out = np.zeros(len(qq[0])); lk = np.zeros(len(qq[0]), np.int32)
+    assert L.ss_host_eri(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq, mode, 1, out, lk) == 0
+print("sanitized run ok")
+"""
+
+
+def test_kernel_arithmetic_under_asan_ubsan(tmp_path):
+    """The kernel's templates (recursion tables, option subsets, light-ket bounds) built for the
+    host with AddressSanitizer, UndefinedBehaviorSanitizer and array-bounds checks, run over every
+    quartet class of the 26-function basis in all three orientations: no report.  The local
+    arrays are the device code's, so this is a bounds check of the kernel's indexing."""
+    import os
+    import sys
+    gxx, nvcc = shutil.which("g++"), shutil.which("nvcc")
+    if gxx is None or nvcc is None:
+        pytest.skip("g++ or the CUDA headers not available")
+    asan = subprocess.run([gxx, "-print-file-name=libasan.so"], capture_output=True, text=True).stdout.strip()
+    if not asan or not Path(asan).exists():
+        pytest.skip("libasan not available")
+    cuda_inc = Path(nvcc).resolve().parent.parent / "include"
+    lib = tmp_path / "liberi_host_san.so"
+    subprocess.run([gxx, "-O1", "-g", "-std=c++17", "-ffp-contract=off", "-Wno-unknown-pragmas", "-shared", "-fPIC",
+                    "-fsanitize=address,undefined,bounds", "-fno-omit-frame-pointer", f"-I{cuda_inc}", f"-I{CSRC}",
+                    str(HERE / "eri_host_shim.cpp"), "-o", str(lib)], check=True)
+    env = dict(os.environ, LD_PRELOAD=asan, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1",
+               UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, "-c", SAN_SCRIPT, str(HERE.parent), str(lib)], env=env,
+                       capture_output=True, text=True, timeout=900, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "sanitized run ok" in r.stdout
+    assert "runtime error" not in r.stderr and "AddressSanitizer" not in r.stderr
