@@ -170,6 +170,13 @@ qq = [np.ascontiguousarray(x, np.int32) for x in q]
 for mode in (0, 1, 2):
     out = np.zeros(len(qq[0])); lk = np.zeros(len(qq[0]), np.int32)
     assert L.ss_host_eri(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq, mode, 1, out, lk) == 0
+# the FP32 templates and boys32 (the FP32 tier), every quartet in the tier's threshold sweep
+from oracle import binding as O
+pre = np.ascontiguousarray(O.precond(O.OracleBasis(b)))
+L.ss_host_fp32_error.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
+                                 i32p, i32p, i32p, i32p, f64p, C.c_double, f64p]
+res = np.zeros(7)
+assert L.ss_host_fp32_error(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq, pre, 1e-6, res) == 0
 print("sanitized run ok")
 """
 
