@@ -161,7 +161,7 @@ L = C.CDLL(sys.argv[2])
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C"); i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
 L.ss_host_eri.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
                           i32p, i32p, i32p, i32p, C.c_int, C.c_int, f64p, i32p]
-b = configs.h2o_26(ng0=2); q = basis.build_mapping(b.n)
+b = configs.h2o_26(ng0=1); q = basis.build_mapping(b.n)
 arrs = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
         np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
         np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
