@@ -195,6 +195,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp32-eps", type=float, default=None,
+                    help="FP32-tier threshold of the analytic stage (ss_set_eri_tiers); default: the library's")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -219,6 +221,8 @@ def main():
     ctx = api.Context(local)
     ctx.set_basis(b)
     ctx.set_quartets(*q)
+    if args.fp32_eps is not None:
+        ctx.set_eri_tiers(1e-18, args.fp32_eps)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     seed = job_seed(1, rank)
@@ -266,6 +270,8 @@ def main():
         c2 = api.Context(local)
         c2.set_basis(b)
         c2.set_quartets(*q)
+        if args.fp32_eps is not None:
+            c2.set_eri_tiers(1e-18, args.fp32_eps)
         eri, sig = c2.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=True)
         e2e_times.append(time.perf_counter() - t)
         c2.close()

@@ -162,6 +162,15 @@ int ss_invalidate(ss_ctx* ctx);
  * reference stops. */
 int ss_monocenter(ss_ctx* ctx, double* out, int32_t* mask, int64_t* n_mono);
 
+/* No counterpart in the reference (it evaluates every primitive quartet in FP64).  Thresholds of
+ * the analytic stage, relative to a quartet's Schwarz bound sqrt((ik|ik)(jl|jl)): a primitive
+ * quartet whose Schwarz bound S_P S_Q is below screen_eps times it is skipped, one below
+ * fp32_eps times it is evaluated in FP32, the rest in FP64.  Defaults 1e-18 and 1e-13;
+ * fp32_eps <= screen_eps (e.g. 0) evaluates every kept primitive quartet in FP64.  Limits:
+ * 0 <= screen_eps <= 1e-18, 0 <= fp32_eps <= 1e-10 (else SS_ERR_ARG).  A change invalidates the
+ * analytic ERIs held by the context; jobs submitted afterwards use the new values. */
+int ss_set_eri_tiers(ss_ctx* ctx, double screen_eps, double fp32_eps);
+
 /* enable != 0: ss_combine, ss_two_e_job and the jobs give the one-centre quartets their exact
  * value with MC mean and error bar 0 (src/two_e_slater.F90:465-494, 558-562). */
 int ss_set_exact_monocenter(ss_ctx* ctx, int enable);
@@ -185,11 +194,14 @@ int ss_split_bf16_gemm(ss_ctx* ctx, int P, int64_t K, const uint16_t* a_hi, cons
  * device memory (their device memory belongs to their own pool, or cudaMalloc is not allowed
  * where they run): it allocates nothing and needs no ss_ctx.  All pointers are DEVICE pointers
  * owned by the caller (A*, B* (P,K) BF16 bits, C (P,P) FP32); stream is a cudaStream_t (NULL =
- * default stream) and the call returns after the stream has finished the work.  The K-slice
- * partials go to a fixed 16 MiB device array inside the library, so P <= 2048 (larger P is
- * rejected with SS_ERR_ARG) and ksplit is reduced to fit.  The first call on a device looks up
- * that array's address; make it before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (other threads, other streams) race and must be serialised. */
+ * default stream).  The call waits for the stream (cudaStreamSynchronize) to read back the
+ * error flag of the bounded device waits, so it returns after the stream has finished the work.
+ * The K-slice partials go to a fixed 16 MiB device array inside the library, so P <= 2048
+ * (larger P is rejected with SS_ERR_ARG) and ksplit is reduced to fit.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) and keeps it; make that
+ * first call before any stream capture.  A device reset (cudaDeviceReset) after that first call
+ * is not supported: the kept address would be stale.  All calls share the array: calls that
+ * overlap on the GPU (other threads, other streams) race and must be serialised. */
 int ss_split_bf16_gemm_noalloc(void* stream, int P, int64_t K, const uint16_t* a_hi,
                                const uint16_t* a_lo, const uint16_t* b_hi, const uint16_t* b_lo,
                                int ksplit, float* c);

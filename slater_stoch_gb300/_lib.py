@@ -68,6 +68,7 @@ SIGNATURES = {
     "ss_psd_project": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_void_p]),
     "ss_monocenter": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ss_set_exact_monocenter": (C.c_int, [C.c_void_p, C.c_int]),
+    "ss_set_eri_tiers": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
     "ss_davidson_clean": (C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
                                     C.c_void_p]),
 }

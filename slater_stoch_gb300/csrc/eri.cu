@@ -178,32 +178,32 @@ void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem) {
   *smem = per * kt;
 }
 
-cudaError_t launch_eri_L0c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L1c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L2c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L2c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L2c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c4(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L3c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
-cudaError_t launch_eri_L4c3k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L0c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L1c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c4(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c0k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c1k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c2k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L4c3k2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 
 // Kernel instance for class (L, tc) and ket bound LK.  tc: number of r^2-type fits among the
 // four functions (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has
@@ -214,35 +214,35 @@ cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
-                             double* partial, double* self_out, const PrimPairF* ppf) {
+                             double eps32, double* partial, double* self_out, const PrimPairF* ppf) {
   if (LK < L) {
 #define SS_KV(LL, TT, KK)                                                                                       \
   if (L == LL && tc == TT && LK == KK)                                                                          \
     return launch_eri_L##LL##c##TT##k##KK(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, \
-                                          pre, eps, partial, self_out, ppf);
+                                          pre, eps, eps32, partial, self_out, ppf);
     SS_KV(3, 0, 1) SS_KV(3, 1, 1) SS_KV(3, 2, 1) SS_KV(4, 0, 1) SS_KV(4, 1, 1) SS_KV(4, 2, 1)
     SS_KV(3, 0, 2) SS_KV(3, 1, 2) SS_KV(3, 2, 2) SS_KV(4, 0, 2) SS_KV(4, 1, 2) SS_KV(4, 2, 2) SS_KV(4, 3, 2)
 #undef SS_KV
     return cudaErrorInvalidValue;
   }
   if (tc == 0) {
-    if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 2) return launch_eri_L2c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 3) return launch_eri_L3c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 4) return launch_eri_L4c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L == 0) return launch_eri_L0c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 1) return launch_eri_L1c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 2) return launch_eri_L2c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c0(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
   } else if (tc == 1) {
-    if (L <= 2) return launch_eri_L2c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 3) return launch_eri_L3c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 4) return launch_eri_L4c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L <= 2) return launch_eri_L2c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c1(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
   } else if (tc == 2) {
-    if (L <= 2) return launch_eri_L2c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 3) return launch_eri_L3c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
-    if (L == 4) return launch_eri_L4c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L <= 2) return launch_eri_L2c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 3) return launch_eri_L3c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
+    if (L == 4) return launch_eri_L4c2(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
   } else if (tc == 3) {
-    if (L <= 4) return launch_eri_L4c3(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L <= 4) return launch_eri_L4c3(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
   } else if (tc == 4) {
-    if (L <= 4) return launch_eri_L4c4(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, partial, self_out, ppf);
+    if (L <= 4) return launch_eri_L4c4(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, pre, eps, eps32, partial, self_out, ppf);
   }
   return cudaErrorInvalidValue;
 }

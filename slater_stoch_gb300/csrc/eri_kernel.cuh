@@ -497,7 +497,8 @@ SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const R
 // is skipped.  Each skipped term is bounded by that product, so the skipped part of an ERI is at
 // most (number of primitive quartets) * eps * sqrt((ik|ik)(jl|jl)).
 // FP32 tier (pre != nullptr): a kept primitive quartet with S_P S_Q < eps32 sqrt((ik|ik)(jl|jl))
-// is evaluated in FP32 (PRIM_FP32_EPS in ss_common.cuh gives the error bound).
+// is evaluated in FP32 (PRIM_FP32_EPS in ss_common.cuh, the default eps32, gives the error
+// bound); eps32 <= eps turns the tier off.
 // For each bra pair the FP64 and the FP32 ket pairs of a tile are consecutive ranges from the
 // start of the tile (the ket factors decrease along it); the items of each tier are numbered
 // through an exclusive scan of the per-bra range lengths.  Without pre every item is FP64 and
@@ -519,7 +520,8 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
     BasisDev B, const PrimPair* __restrict__ pp, const int64_t* __restrict__ pair_off,
     const int* __restrict__ pair_cnt, const int64_t* __restrict__ work, int split, int ktile,
     const int32_t* __restrict__ is, const int32_t* __restrict__ js, const int32_t* __restrict__ ks,
-    const int32_t* __restrict__ ls, const double* __restrict__ pre, double eps, double* __restrict__ partial,
+    const int32_t* __restrict__ ls, const double* __restrict__ pre, double eps, double eps32,
+    double* __restrict__ partial,
     double* __restrict__ self_out, const PrimPairF* __restrict__ ppf) {
   constexpr bool T2 = TC > 0;
   constexpr int NO = T2 ? 4 : 1;        // options per axis: which of the pair's functions adds +2
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
   const double sch = pre ? sqrt(pre[fi + (int64_t)n * fk] * pre[fj + (int64_t)n * fl]) : 0.0;
   // the FP32 tier needs the Schwarz diagonal and the FP32 pair copies (not in self mode)
   const bool fp32_tier = pre != nullptr && ppf != nullptr && self_out == nullptr;
-  const double tau = eps * sch, tau32 = fp32_tier ? PRIM_FP32_EPS * sch : 0.0;
+  const double tau = eps * sch, tau32 = (fp32_tier && eps32 > eps) ? eps32 * sch : 0.0;
 
   const int per = (nb + split - 1) / split;
   const int b0 = part * per;
@@ -604,7 +606,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
           return lo;
         };
         c = first_below(tau);
-        c64 = first_below(tau32);
+        c64 = tau32 > tau ? first_below(tau32) : c;  // no FP32 tier: every kept item in FP64
       }
       s_scan[bi + 1] = c64;
       s_scan32[bi + 1] = c - c64;

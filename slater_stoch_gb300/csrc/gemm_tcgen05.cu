@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
+  int issued = 0;  // stages the producer filled (read by the producer lane only)
   if (warp == 0 && lane == 0) {
     // TMA producer
     for (int t = 0; t < nkt; t++) {
@@ -159,10 +160,10 @@ __global__ void __launch_bounds__(128, 1)
       tma_load_2d(&tAlo, st + TILE_BYTES, &full_bar[s], x, tm * BM);
       tma_load_2d(&tBhi, st + 2 * TILE_BYTES, &full_bar[s], x, tn * BN);
       tma_load_2d(&tBlo, st + 3 * TILE_BYTES, &full_bar[s], x, tn * BN);
+      issued = t + 1;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    int issued = 0;
     for (int t = 0; t < nkt; t++) {
       const int s = t % STAGES;
       const uint32_t ph = (uint32_t)((t / STAGES) & 1);
@@ -185,10 +186,8 @@ __global__ void __launch_bounds__(128, 1)
         mma_bf16(tmem, alo, bhi, 1u);
       }
       mma_commit(&empty_bar[s]);  // frees the stage once these MMAs have read it
-      issued++;
     }
     mma_commit(acc_bar);  // arrives once every issued MMA has completed
-    (void)issued;
   }
   __syncwarp();
 
@@ -223,6 +222,17 @@ __global__ void __launch_bounds__(128, 1)
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  // After an abort, TMA loads the MMA warp never consumed may still be writing into shared
+  // memory: the producer waits (bounded) for the last load of every stage before the CTA exits.
+  // Stage s last received load t = issued-1-((issued-1-s) mod STAGES); its phase parity is
+  // (t / STAGES) & 1 and no later load was issued into it, so the parity wait is unambiguous.
+  if (warp == 0 && lane == 0 && *(volatile int*)&s_abort) {
+    for (int s = 0; s < STAGES && s < issued; s++) {
+      const int t = issued - 1 - ((issued - 1 - s) % STAGES);
+      if (!mbar_wait(&full_bar[s], (uint32_t)((t / STAGES) & 1))) atomicExch(err, ERR_FULL_WAIT);
+    }
+  }
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
@@ -371,11 +381,9 @@ int launch_split_bf16_gemm(cudaStream_t st, const void* a_hi, const void* a_lo, 
   const int ktiles = (int)(K / BK);
   const int per = (ktiles + ksplit - 1) / ksplit;
   const int T = (P + BM - 1) / BM;
-  static bool attr_set = false;
-  if (!attr_set) {
-    SS_CUDA_TRY(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
-  }
+  // the dynamic shared-memory opt-in is held per device: set it before every launch (cheap), so
+  // any device and any thread launching here has it, with no process-wide flag to race on
+  SS_CUDA_TRY(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   dim3 grid((unsigned)T, (unsigned)T, (unsigned)ksplit);
   split_bf16_gemm_kernel<<<grid, 128, SMEM_BYTES, st>>>(mAhi, mAlo, mBhi, mBlo, P, ktiles, per, c_partial, err_flag);
   SS_CUDA_TRY(cudaGetLastError());

@@ -75,6 +75,7 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
   std::vector<int32_t> is = c->h_is, jsv = c->h_js, ks = c->h_ks, ls = c->h_ls;
   const int64_t nint = c->nint;
   const bool exact_mono = c->exact_monocenter;
+  const double eps_screen = c->eri_eps_screen, eps32 = c->eri_eps32;
   JobState* st = js.get();
   try {
     js->th = std::thread([=]() {
@@ -86,6 +87,7 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
                           gg.data(), gs.data());
       if (!rc) rc = ss_quartets_set(w, nint, is.data(), jsv.data(), ks.data(), ls.data());
       if (!rc) rc = ss_set_exact_monocenter(w, exact_mono ? 1 : 0);
+      if (!rc) rc = ss_set_eri_tiers(w, eps_screen, eps32);
       if (!rc)
         rc = ss_two_e_job(w, a_zv, seed, samples_per_block, nblocks, estimator, precision, sigma_target,
                           st->eri.data(), st->sigma.data());

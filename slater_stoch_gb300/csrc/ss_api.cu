@@ -20,7 +20,7 @@ cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
                              const int32_t* ks, const int32_t* ls, const double* pre, double eps,
-                             double* partial, double* self_out, const PrimPairF* ppf);
+                             double eps32, double* partial, double* self_out, const PrimPairF* ppf);
 __global__ void prim_pair_to_f32(int64_t npp, const PrimPair* in, PrimPairF* out);
 __global__ void prim_pair_sort(const PrimPair* in, const int64_t* off, const int* cnt, PrimPair* out);
 __global__ void prim_pair_count(BasisDev B, int npairs, int* cnt);
@@ -121,7 +121,7 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const int32_t* d_qls, const std::vector<int32_t>& qis, const std::vector<int32_t>& qjs,
                    const std::vector<int32_t>& qks, const std::vector<int32_t>& qls,
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
-                   const double* d_pre, double eps, double* self_out = nullptr) {
+                   const double* d_pre, double eps, double eps32, double* self_out = nullptr) {
   // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
   // functions) and, for L >= 3, the light-ket variant v: the lighter pair has L <= v (v = 1, 2;
   // v = 0 for the others).  A light-ket quartet is evaluated as (jl|ik) when (j,l) is the
@@ -210,7 +210,7 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
       cudaError_t e = launch_eri_class(L, LK, tc, grid, ktile, smem, st, c->basis,
                                        (const PrimPair*)c->d_pp.ptr, (const int64_t*)c->d_pp_off.ptr,
                                        (const int*)c->d_pp_cnt.ptr, d_work + begin[bk] + s0, split, d_qis,
-                                       d_qjs, d_qks, d_qls, d_pre, eps, d_partial + pbase[bk] + s0 * split,
+                                       d_qjs, d_qks, d_qls, d_pre, eps, eps32, d_partial + pbase[bk] + s0 * split,
                                        self_out, (const PrimPairF*)c->d_ppf.ptr);
       if (e != cudaSuccess) {
         ss_set_cuda_error(e, "eri_kernel launch", __FILE__, __LINE__);
@@ -289,12 +289,12 @@ int ensure_precond(ss_ctx* c) {
   // 2. per-pair sort by decreasing factor, 3. the diagonal quartets themselves
   if (!rc)
     rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
-                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0,
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0, 0.0,
                  (double*)((char*)c->d_pp.ptr + offsetof(PrimPair, pad)));
   if (!rc) rc = sort_prim_pairs(c);
   if (!rc)
     rc = run_eri(c, (const int32_t*)di.ptr, (const int32_t*)di.ptr, (const int32_t*)dk.ptr,
-                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0);
+                 (const int32_t*)dk.ptr, qi, qi, qk, qk, sel, slot, npartial, nullptr, 0.0, 0.0);
   if (rc) {
     dev_free(c, di);
     dev_free(c, dk);
@@ -354,7 +354,7 @@ int ensure_gauss(ss_ctx* c) {
   int64_t npartial = 0;
   rc = run_eri(c, (const int32_t*)c->d_is.ptr, (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
                (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, npartial,
-               (const double*)c->d_precond.ptr, PRIM_SCREEN_EPS);
+               (const double*)c->d_precond.ptr, c->eri_eps_screen, c->eri_eps32);
   if (rc) return rc;
   rc = h2d(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
   if (rc) return rc;
@@ -392,6 +392,26 @@ const char* ss_strerror(int code) {
 }
 
 const char* ss_last_error(void) { return g_err.c_str(); }
+
+int ss_set_eri_tiers(ss_ctx* c, double screen_eps, double fp32_eps) {
+  if (!c) {
+    ss_set_error_msg("null ss_ctx");
+    return SS_ERR_ARG;
+  }
+  // the screen's skipped part of an ERI is below 900^2 * screen_eps of its Schwarz bound, so
+  // 1e-18 keeps it under 1e-12; the FP32 tier's error grows ~linearly with fp32_eps (measured
+  // sums of |FP32 - FP64| over a quartet's tier: 1.6e-17 at 1e-13, 1.8e-15 at 1e-11, 1.8e-14
+  // at 1e-10 of the Schwarz bound at 20-Gaussian fits)
+  if (!(screen_eps >= 0.0 && screen_eps <= 1e-18) || !(fp32_eps >= 0.0 && fp32_eps <= 1e-10)) {
+    ss_set_error_msg("ss_set_eri_tiers: need 0 <= screen_eps <= 1e-18 and 0 <= fp32_eps <= 1e-10 (got %g, %g)",
+                     screen_eps, fp32_eps);
+    return SS_ERR_ARG;
+  }
+  if (c->eri_eps_screen != screen_eps || c->eri_eps32 != fp32_eps) c->have_gauss = false;
+  c->eri_eps_screen = screen_eps;
+  c->eri_eps32 = fp32_eps;
+  return SS_OK;
+}
 
 ss_ctx* ss_create(int device, size_t hbm_budget) {
   int ndev = 0;

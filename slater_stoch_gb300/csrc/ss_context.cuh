@@ -79,6 +79,8 @@ struct ss_ctx {
 
   // analytic results
   bool have_precond = false, have_gauss = false;
+  // primitive screening and FP32-tier thresholds of the analytic stage (ss_set_eri_tiers)
+  double eri_eps_screen = ss::PRIM_SCREEN_EPS, eri_eps32 = ss::PRIM_FP32_EPS;
   std::vector<double> h_precond;
   ss::DevBuf d_precond, d_gauss;
   int64_t n_removed = 0;

@@ -9,8 +9,10 @@ script extracts them verbatim into a plain text table
 
     n  m  c_fit  g_fit
 
-one row per (n, m), m = 1..n.  Run it in a container that has the reference
-checkout (path given as the first argument, default ``/root/reference``).
+one row per (n, m), m = 1..n.  Run it where a checkout of the reference exists:
+
+    python gen_sto_fits.py <path of the reference checkout>
+
 The generated file is committed; nothing reads the reference at run time.
 """
 import re
@@ -18,7 +20,7 @@ import sys
 from pathlib import Path
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str) -> None:
     src = Path(ref_root) / "src" / "read_fit_SMILES.F90"
     text = src.read_text()
     pat = re.compile(r"([cg])_fit_exp\(\s*(\d+)\s*,\s*(\d+)\s*\)\s*=\s*([-+0-9.DdEe]+)")
@@ -40,4 +42,6 @@ def main(ref_root: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python gen_sto_fits.py <path of the reference checkout>")
+    main(sys.argv[1])

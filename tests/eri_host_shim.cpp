@@ -3,6 +3,7 @@
 // the Boys tables), with the device's choice of template instance and light-ket orientation,
 // over all primitive pairs (no screening, FP64 only).  The primitive pairs are built as
 // prim_pair_fill builds them (csrc/eri.cu), including the folding of same-fit pairs.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -341,6 +342,64 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
   out[5] = e.q_abs;
   out[6] = e.q_acc;
   return 0;
+}
+
+// Per quartet: the template instance the device runs (L, LK, tc) and how its primitive quartets
+// split into the kernel's three tiers, from the same pair records and Schwarz factors S_P as the
+// device (no integral is evaluated): counts[4q + 0] screened (S_P S_Q < eps_screen * sch),
+// [4q + 1] FP32 tier (eps_screen * sch <= S_P S_Q < eps32 * sch), [4q + 2] FP64, [4q + 3] all,
+// with sch = sqrt((ik|ik)(jl|jl)) from pre (n x n column-major).  cls[3q..3q+2] = L, LK, tc.
+int ss_host_tier_counts(int n, int ld, const double* center, const int* npower, const int* nsto, const int* itype,
+                        const int* ng, const double* cg, const double* gg, const double* gs, int64_t nint,
+                        const int32_t* is, const int32_t* js, const int32_t* ks, const int32_t* ls,
+                        const double* pre, double eps_screen, double eps32, double* counts, int* cls) {
+  BasisDev B{n, ld, center, npower, nsto, itype, ng, cg, gg, gs};
+  std::vector<std::vector<double>> fac((size_t)n * (n + 1) / 2);
+  std::vector<char> have(fac.size(), 0);
+  int bad = 0;
+  auto factors = [&](int i, int k) -> const std::vector<double>& {
+    if (i < k) std::swap(i, k);
+    const size_t p = (size_t)ss_pair_index(i, k);
+    if (!have[p]) {
+      std::vector<double> f = schwarz(B, i, k, build_pairs(B, i, k, true), &bad);
+      std::sort(f.begin(), f.end(), [](double a, double b) { return a > b; });
+      fac[p] = std::move(f);
+      have[p] = 1;
+    }
+    return fac[p];
+  };
+  // number of (b, t) with Sb[b] * Sk[t] >= thr, both lists in decreasing order (two pointers)
+  auto count_ge = [](const std::vector<double>& Sb, const std::vector<double>& Sk, double thr) {
+    double c = 0.0;
+    size_t hi = Sk.size();  // kets [0, hi) pass for the current bra; hi shrinks as Sb decreases
+    for (size_t b = 0; b < Sb.size(); b++) {
+      while (hi > 0 && !(Sb[b] * Sk[hi - 1] >= thr)) hi--;
+      c += (double)hi;
+    }
+    return c;
+  };
+  for (int64_t q = 0; q < nint; q++) {
+    int i = is[q] - 1, k = ks[q] - 1, j = js[q] - 1, l = ls[q] - 1;
+    const int Lb = pair_L(B, i, k), Lk = pair_L(B, j, l);
+    const int L = std::max(Lb, Lk);
+    const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
+    const int lmin = std::min(Lb, Lk);
+    const int v = (L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    cls[3 * q] = L;
+    cls[3 * q + 1] = v ? v : L;
+    cls[3 * q + 2] = tc;
+    const double sch = std::sqrt(pre[i + (int64_t)n * k] * pre[j + (int64_t)n * l]);
+    const std::vector<double>& Sb = factors(i, k);
+    const std::vector<double>& Sk = factors(j, l);
+    const double all = (double)Sb.size() * (double)Sk.size();
+    const double kept = count_ge(Sb, Sk, eps_screen * sch);
+    const double f64 = count_ge(Sb, Sk, eps32 * sch);
+    counts[4 * q] = all - kept;
+    counts[4 * q + 1] = kept - f64;
+    counts[4 * q + 2] = f64;
+    counts[4 * q + 3] = all;
+  }
+  return bad;
 }
 
 }  // extern "C"

@@ -52,6 +52,75 @@ def test_gauss_eri_full_small_fits(cfg, ng0):
     _check(g, ref, pre, q)
 
 
+def _stratified(counts, cls, per_class=40, top_fp32=50, seed=20):
+    """>= per_class quartets of every kernel instance (L, LK, tc) (all of a smaller class) and the
+    top_fp32 quartets with the largest FP32-tier share of their kept primitive quartets."""
+    rng = np.random.default_rng(seed)
+    keys = cls[:, 0] * 100 + cls[:, 1] * 10 + cls[:, 2]
+    sel = set()
+    for key in np.unique(keys):
+        idx = np.nonzero(keys == key)[0]
+        sel.update(rng.choice(idx, min(per_class, idx.size), replace=False).tolist())
+    kept = counts[:, 1] + counts[:, 2]
+    share = np.where(kept > 0, counts[:, 1] / np.maximum(kept, 1), 0.0)
+    sel.update(np.argsort(-share, kind="stable")[:top_fp32].tolist())
+    return np.array(sorted(sel)), share
+
+
+@pytest.fixture(scope="module")
+def h2o26_ng20(tmp_path_factory):
+    """The benchmarked workload: 26-function H2O basis, 20-Gaussian fits, all 61,776 quartets on
+    the device (screening and the FP32 tier on); the oracle's Schwarz diagonal and the kernel's
+    own tier split of every quartet (host build of the kernel arithmetic)."""
+    import eri_host
+    if not eri_host.available():
+        pytest.fail("g++ and the CUDA headers are needed to build the kernel's host arithmetic")
+    O = _oracle()
+    b = configs.h2o_26(ng0=20)
+    q = basis.build_mapping(b.n)
+    ob = O.OracleBasis(b)
+    pre = O.precond(ob)
+    L = eri_host.load(eri_host.build(tmp_path_factory.mktemp("erihost")))
+    return O, b, q, ob, pre, L, {}  # the last: oracle values by quartet index, shared by the cases
+
+
+@pytest.mark.parametrize("fp32_eps", [1e-13, 1e-11])
+def test_gauss_eri_h2o26_ng20_stratified(h2o26_ng20, fp32_eps):
+    """All 61,776 ERIs of the benchmarked configuration computed on the device; compared with the
+    oracle on the whole Schwarz diagonal (351 quartets (ik|ik)), a stratified sample of >= 40
+    quartets from every kernel instance (L, LK, tc), and the 50 quartets whose kept primitive
+    quartets go most to the FP32 tier.  Gate per quartet: 1e-12 |ERI| + 1e-12 sqrt((ik|ik)(jl|jl)).
+    Run at the default FP32-tier threshold (1e-13 of the Schwarz bound) and at 1e-11."""
+    import eri_host
+    O, b, q, ob, pre, L, memo = h2o26_ng20
+    counts, cls = eri_host.tier_counts(L, b, q, pre, 1e-18, fp32_eps)
+    qa = [np.asarray(a) for a in q]
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*q)
+        ctx.set_eri_tiers(1e-18, fp32_eps)
+        gp = ctx.precond()
+        g, nz = ctx.gauss_eri()
+    np.testing.assert_allclose(gp.reshape(-1, order="F"), pre, rtol=RTOL, atol=0)
+    sel, share = _stratified(counts, cls)
+    sub = [a[sel] for a in qa]
+    todo = np.array([t for t in sel if t not in memo], dtype=np.int64)
+    if todo.size:
+        vals, _ = O.gauss_eri(ob, [a[todo] for a in qa], pre)
+        memo.update(zip(todo.tolist(), vals.tolist()))
+    ref = np.array([memo[t] for t in sel.tolist()])
+    n = b.n
+    P = pre.reshape(n, n, order="F")
+    i, j, k, l = [a - 1 for a in sub]
+    bound = RTOL * np.abs(ref) + RTOL * np.sqrt(np.abs(P[i, k] * P[j, l]))
+    ratio = np.abs(g[sel] - ref) / bound
+    worst = int(np.argmax(ratio))
+    print(f"\nh2o_26 ng0=20 fp32_eps={fp32_eps:g}: {sel.size} quartets vs oracle, worst |gpu-oracle|/gate "
+          f"{ratio[worst]:.3e} (quartet {[int(x[worst]) for x in sub]}, FP32 share {share[sel][worst]:.2f}); "
+          f"largest FP32 share in the sample {share[sel].max():.3f}")
+    assert np.all(ratio <= 1.0), f"{(ratio > 1).sum()} quartets outside the gate, worst ratio {ratio.max():.3g}"
+
+
 def test_gauss_eri_golden_ng20():
     """20-Gaussian fits (the production setting) against the committed oracle fixture."""
     from pathlib import Path

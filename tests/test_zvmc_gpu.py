@@ -24,9 +24,22 @@ def _setup(cfg, ng0):
     return b, q
 
 
+_PRE = {}
+
+
+def _oracle_precond(O, ob, key):
+    if key not in _PRE:
+        O.set_sum_mode("extended")
+        _PRE[key] = O.precond(ob)
+    return _PRE[key]
+
+
 @pytest.mark.parametrize("precision,rtol", [("fp64", 1e-10), ("ref32", 1e-9)])
-@pytest.mark.parametrize("cfg,ng0", [("h2o_minimal", 4), ("h2o_minimal", 20)])
+@pytest.mark.parametrize("cfg,ng0", [("h2o_minimal", 4), ("h2o_minimal", 20), ("h2o_26", 20)])
 def test_faithful_vs_oracle(cfg, ng0, precision, rtol):
+    """h2o_26 with 20-Gaussian fits is the benchmarked workload (61,776 quartets); there the
+    |ERI| in the gate's relative term is the device's analytic value, which the analytic parity
+    tests hold to 1e-12 of the oracle."""
     from oracle import binding as O
     b, q = _setup(cfg, ng0)
     nblocks, npts = 3, 4000
@@ -37,11 +50,11 @@ def test_faithful_vs_oracle(cfg, ng0, precision, rtol):
         r1, r2 = ctx.draw_walkers(seed=7, first=0, S=nblocks * npts)
         # same walkers through the host-walker entry point
         mean_w, sigma_w = ctx.zvmc_walkers(1.8, r1, r2, npts, nblocks, precision)
+        g_dev, _ = ctx.gauss_eri() if cfg == "h2o_26" else (None, 0)
     ob = O.OracleBasis(b)
     ref, err = O.zvmc_faithful(ob, q, 1.8, r1, r2, nblocks, npts, precision)
-    O.set_sum_mode("extended")
-    pre = O.precond(ob).reshape(b.n, b.n, order="F")
-    gauss, _ = O.gauss_eri(ob, q, pre.reshape(-1, order="F"))
+    pre = _oracle_precond(O, ob, (cfg, ng0)).reshape(b.n, b.n, order="F")
+    gauss = g_dev if g_dev is not None else O.gauss_eri(ob, q, pre.reshape(-1, order="F"))[0]
     i, j, k, l = [np.asarray(a) - 1 for a in q]
     schwarz = np.sqrt(np.abs(pre[i, k] * pre[j, l]))
     bound = rtol * np.abs(gauss + ref) + 1e-14 * schwarz
@@ -103,7 +116,11 @@ def test_shared_estimator_sto_1s_known_answer(zeta):
 
 def test_shared_agrees_with_faithful():
     """Both estimators are unbiased for the same correction: on the 7-function H2O basis with
-    4-Gaussian fits (corrections ~1e-2 Ha) they agree within 5 combined sigma for all 406 ERIs."""
+    4-Gaussian fits (corrections ~1e-2 Ha), two independent runs (different seeds, different
+    estimators) agree within 3 combined sigma.  With 406 integrals and |z| ~ N(0,1), about
+    406 * 0.0027 = 1.1 exceed 3 sigma; the gate allows at most 6 exceedances (the chance of
+    more is ~1e-4 for independent integrals), none beyond 5 sigma, and mean |z| < 1.2 (|N(0,1)|
+    averages 0.80)."""
     b, q = _setup("h2o_minimal", 4)
     with api.Context(0) as ctx:
         ctx.set_basis(b)
@@ -113,5 +130,7 @@ def test_shared_agrees_with_faithful():
         mf, sf = ctx.zvmc(a_zv=1.8, seed=22, npts=40 * 400, nblocks=16, estimator="faithful",
                           precision="fp64")
     z = np.abs(ms - mf) / np.sqrt(ss ** 2 + sf ** 2 + 1e-300)
+    n3 = int((z > 3.0).sum())
+    assert n3 <= 6, f"{n3} of {z.size} integrals beyond 3 sigma (expected ~1.1), max |z| {z.max():.2f}"
     assert np.all(z <= 5.0), f"max |z| {z.max():.2f}"
-    assert np.mean(z) < 1.2  # |N(0,1)| averages 0.80
+    assert np.mean(z) < 1.2
