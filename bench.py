@@ -348,7 +348,7 @@ def main():
             "metric": METRIC,
             "value": value, "unit": "ERIs/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": ("f64 analytic (f32 for primitive quartets below 1e-13 of their Schwarz bound) + "
+            "dtype": ("f64 analytic (f32 for primitive quartets below 1e-11 of their Schwarz bound) + "
                       "bf16x3 (fp32 accumulate) MC"), "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "walkers": args.walkers, "blocks": NBLOCKS, "estimator": "shared-walker, split-BF16",

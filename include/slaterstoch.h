@@ -165,7 +165,7 @@ int ss_monocenter(ss_ctx* ctx, double* out, int32_t* mask, int64_t* n_mono);
 /* No counterpart in the reference (it evaluates every primitive quartet in FP64).  Thresholds of
  * the analytic stage, relative to a quartet's Schwarz bound sqrt((ik|ik)(jl|jl)): a primitive
  * quartet whose Schwarz bound S_P S_Q is below screen_eps times it is skipped, one below
- * fp32_eps times it is evaluated in FP32, the rest in FP64.  Defaults 1e-18 and 1e-13;
+ * fp32_eps times it is evaluated in FP32, the rest in FP64.  Defaults 1e-18 and 1e-11;
  * fp32_eps <= screen_eps (e.g. 0) evaluates every kept primitive quartet in FP64.  Limits:
  * 0 <= screen_eps <= 1e-18, 0 <= fp32_eps <= 1e-10 (else SS_ERR_ARG).  A change invalidates the
  * analytic ERIs held by the context; jobs submitted afterwards use the new values. */

@@ -88,7 +88,7 @@ class Context:
         _lib.check(self._L.ss_precond(self._h, _ptr(out)))
         return out.reshape(self.n, self.n, order="F")
 
-    def set_eri_tiers(self, screen_eps: float = 1e-18, fp32_eps: float = 1e-13):
+    def set_eri_tiers(self, screen_eps: float = 1e-18, fp32_eps: float = 1e-11):
         """Primitive-quartet screen and FP32-tier thresholds of the analytic stage, relative to
         each quartet's Schwarz bound (ss_set_eri_tiers)."""
         _lib.check(self._L.ss_set_eri_tiers(self._h, float(screen_eps), float(fp32_eps)))

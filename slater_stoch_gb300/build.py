@@ -57,7 +57,7 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     if LIB.exists() and LIB.stat().st_mtime >= newest:
         return LIB
     tmp = LIB.with_suffix(f".{os.getpid()}.so")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcublas", "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -11,12 +11,15 @@
 // components it cannot resolve relative to the largest one fail the sign test and are found
 // in later passes, after the deflation has removed the large ones.
 //
+// Every product is the hand-written FP64 dgemm of linalg.cu, the orthonormalisations its blocked
+// Householder QR and the eigenproblems its eigensolvers; each svd_clean pass reads back one
+// small record (sign-test counts, largest |D|) to decide whether another pass is needed.
+//
 // ss_davidson restates src/davidson.F90:1-158 (lowest m eigenpairs, NMAX = min(10, N/m),
 // diagonal preconditioner (E u - H u)/max(H_ii - E, 1e-2), convergence when the largest
 // correction norm is < tol); the basis is kept orthonormal so the projected problem is a
 // standard symmetric eigenproblem (the reference solves the equivalent generalized one with
 // dsygv).
-#include <cublas_v2.h>
 #include <math.h>
 #include <string.h>
 
@@ -36,30 +39,6 @@ namespace ss {
     int _rc = (x);       \
     if (_rc) return _rc; \
   } while (0)
-#define CUBLAS_TRY(x)                                                       \
-  do {                                                                      \
-    cublasStatus_t _s = (x);                                                \
-    if (_s != CUBLAS_STATUS_SUCCESS) {                                      \
-      ss_set_error_msg("cuBLAS error %d at %s:%d", (int)_s, __FILE__, __LINE__); \
-      return SS_ERR_CUDA;                                                   \
-    }                                                                       \
-  } while (0)
-
-static int get_cublas(ss_ctx* c, cublasHandle_t* h) {
-  if (!c->cublas_handle) {
-    cublasHandle_t hh;
-    CUBLAS_TRY(cublasCreate(&hh));
-    CUBLAS_TRY(cublasSetStream(hh, c->stream));
-    c->cublas_handle = (void*)hh;
-  }
-  *h = (cublasHandle_t)c->cublas_handle;
-  return SS_OK;
-}
-
-void destroy_cublas(void* h) {
-  if (h) cublasDestroy((cublasHandle_t)h);
-}
-
 // ---------------------------------------------------------------------------------------
 // scatter / gather between the quartet list and the symmetric matrix
 // ---------------------------------------------------------------------------------------
@@ -183,23 +162,64 @@ __global__ void scale_rows_kernel(int r, int N, double* __restrict__ Vt, const d
   Vt[e] *= inv[e % r];
 }
 
-// reverse column order of a (n x n row-major eigenvectors) into out col-major (largest first)
-__global__ void reverse_eigvec_kernel(int n, const double* __restrict__ a, double* __restrict__ out) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= (int64_t)n * n) return;
-  const int row = (int)(e % n), col = (int)(e / n);  // out col-major (row, col)
-  out[e] = a[(size_t)row * n + (n - 1 - col)];
-}
-
-__global__ void transpose_sym_kernel(int n, const double* __restrict__ in, double* __restrict__ out) {
-  // out row-major = symmetrised in (col-major)
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= (int64_t)n * n) return;
-  const int i = (int)(e / n), j = (int)(e % n);
-  out[e] = 0.5 * (in[i + (size_t)j * n] + in[j + (size_t)i * n]);
-}
-
 static unsigned nb(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+// reverse the column order of the ascending eigenvectors V (r x r) into UY (largest first) and
+// the singular values D_k = sqrt(max(ev[r-1-k], 0)) with their inverses
+__global__ void svd_uy_kernel(int r, const double* __restrict__ V, const double* __restrict__ ev,
+                              double* __restrict__ UY, double* __restrict__ D, double* __restrict__ invD) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)r * r) return;
+  const int i = (int)(e % r), k = (int)(e / r);
+  UY[e] = V[i + (size_t)(r - 1 - k) * r];
+  if (i == 0) {
+    const double d = sqrt(fmax(ev[r - 1 - k], 0.0));
+    D[k] = d;
+    invD[k] = d > 0.0 ? 1.0 / d : 0.0;
+  }
+}
+
+struct SvdPassStats {
+  int nbad, nneg;
+  double dmax;
+};
+
+// the sign test of src/svd_clean.F90:286-296 on the device: D_k takes the sign of
+// r_k = <U_k, Vt_k>, components with |r_k| < 0.99 are dropped; absD / negD are the deflation
+// weights of W_work and W.  One CTA.
+__global__ void svd_sign_kernel(int r, const double* __restrict__ rk, const double* __restrict__ D,
+                                double* __restrict__ absD, double* __restrict__ negD, SvdPassStats* st) {
+  __shared__ int s_bad, s_neg;
+  __shared__ double s_max[32];
+  if (threadIdx.x == 0) {
+    s_bad = 0;
+    s_neg = 0;
+  }
+  __syncthreads();
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < r; k += blockDim.x) {
+    double d = rk[k] < 0.0 ? -D[k] : D[k];
+    if (fabs(rk[k]) < 0.99) {
+      d = 0.0;
+      atomicAdd(&s_bad, 1);
+    }
+    if (d < 0.0) atomicAdd(&s_neg, 1);
+    absD[k] = fabs(d);
+    negD[k] = d < 0.0 ? d : 0.0;
+    mx = fmax(mx, fabs(d));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmax(m, s_max[w]);
+    st->nbad = s_bad;
+    st->nneg = s_neg;
+    st->dmax = m;
+  }
+}
 
 int psd_clean(ss_ctx* c, double* moy_host, int layout, int rank, int oversample, int q, uint64_t seed,
               int* n_removed) {
@@ -211,35 +231,39 @@ int psd_clean(ss_ctx* c, double* moy_host, int layout, int rank, int oversample,
   }
   const int N = (int)N64;
   const int r = std::min(rank + oversample, N);
-  if (r < 1 || r > 1024) {
-    ss_set_error_msg("psd_clean: rank + oversample must be in 1..1024 (got %d)", r);
+  if (r < 1 || r > 2048) {
+    ss_set_error_msg("psd_clean: rank + oversample must be in 1..2048 (got %d)", r);
     return SS_ERR_ARG;
   }
-  cublasHandle_t hb;
-  TRY(get_cublas(c, &hb));
   void* p;
-  double *W, *Ww, *P, *Z, *Qw, *tau, *Y, *G, *ev, *ework, *UY, *U, *Vt, *Us, *Dd, *rk, *moy;
-  int* info;
+  double *W, *Ww, *P, *Z, *Y, *G, *ev, *UYv, *UY, *U, *Vt, *Us, *D, *invD, *absD, *negD, *rk, *moy, *qrw, *eigw, *gws;
   const size_t NN = (size_t)N * N, Nr = (size_t)N * r, rr = (size_t)r * r;
+  const size_t gsz = std::max({dgemm_ws(N, r, N), dgemm_ws(r, N, N), dgemm_ws(r, r, N), dgemm_ws(r, N, r),
+                               dgemm_ws(N, r, r), dgemm_ws(N, N, r), (size_t)1});
   TRY(pool_get(c, "cl_W", sizeof(double) * NN, &p)); W = (double*)p;
   TRY(pool_get(c, "cl_Ww", sizeof(double) * NN, &p)); Ww = (double*)p;
   TRY(pool_get(c, "cl_P", sizeof(double) * Nr, &p)); P = (double*)p;
   TRY(pool_get(c, "cl_Z", sizeof(double) * Nr, &p)); Z = (double*)p;
-  TRY(pool_get(c, "cl_Qw", sizeof(double) * Nr, &p)); Qw = (double*)p;
-  TRY(pool_get(c, "cl_tau", sizeof(double) * r, &p)); tau = (double*)p;
   TRY(pool_get(c, "cl_Y", sizeof(double) * Nr, &p)); Y = (double*)p;
   TRY(pool_get(c, "cl_G", sizeof(double) * rr, &p)); G = (double*)p;
   TRY(pool_get(c, "cl_ev", sizeof(double) * r, &p)); ev = (double*)p;
-  TRY(pool_get(c, "cl_ework", sizeof(double) * 2 * r, &p)); ework = (double*)p;
+  TRY(pool_get(c, "cl_UYv", sizeof(double) * rr, &p)); UYv = (double*)p;
   TRY(pool_get(c, "cl_UY", sizeof(double) * rr, &p)); UY = (double*)p;
   TRY(pool_get(c, "cl_U", sizeof(double) * Nr, &p)); U = (double*)p;
   TRY(pool_get(c, "cl_Vt", sizeof(double) * Nr, &p)); Vt = (double*)p;
   TRY(pool_get(c, "cl_Us", sizeof(double) * Nr, &p)); Us = (double*)p;
-  TRY(pool_get(c, "cl_D", sizeof(double) * r, &p)); Dd = (double*)p;
-  TRY(pool_get(c, "cl_rk", sizeof(double) * r, &p)); rk = (double*)p;
+  TRY(pool_get(c, "cl_D", sizeof(double) * 5 * r, &p)); D = (double*)p;
+  invD = D + r; absD = D + 2 * r; negD = D + 3 * r; rk = D + 4 * r;
   TRY(pool_get(c, "cl_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
-  TRY(pool_get(c, "cl_info", sizeof(int), &p)); info = (int*)p;
+  TRY(pool_get(c, "cl_qr", sizeof(double) * ortho_qr_ws(N, r), &p)); qrw = (double*)p;
+  TRY(pool_get(c, "cl_eig", sizeof(double) * std::max<size_t>(sym_eig_ws(r), 1), &p)); eigw = (double*)p;
+  TRY(pool_get(c, "cl_gws", sizeof(double) * gsz, &p)); gws = (double*)p;
+  TRY(pool_get(c, "cl_stats", 64, &p));
+  SvdPassStats* dstats = (SvdPassStats*)p;
+  int* derr = (int*)((char*)p + 32);
+  int64_t* L = &c->launches;
   cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), st));
   SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
   SS_CUDA_TRY(cudaMemsetAsync(Ww, 0, sizeof(double) * NN, st));
   scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
@@ -247,80 +271,59 @@ int psd_clean(ss_ctx* c, double* moy_host, int layout, int rank, int oversample,
                                                (const int32_t*)c->d_ls.ptr, moy, Ww);
   SS_CUDA_TRY(cudaGetLastError());
   SS_CUDA_TRY(cudaMemcpyAsync(W, Ww, sizeof(double) * NN, cudaMemcpyDeviceToDevice, st));
-  c->launches++;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
+  (*L)++;
   int npass = 0, removed = 0;
   uint32_t pass = 0;
-  std::vector<double> hD(r), hR(r), hev(r);
   while (npass < N) {
     gaussian_matrix_kernel<<<r, 256, 0, st>>>(seed, pass, N, r, P);
     SS_CUDA_TRY(cudaGetLastError());
-    // Z = W_work P; orthonormalise
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, N, &one, Ww, N, P, N, &zero, Z, N));
-    TRY(ortho_qr(st, N, r, Z, N, Qw, tau, &c->launches));
-    for (int it = 0; it < q; it++) {  // power iterations (src/svd_clean.F90:212-255)
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, N, r, N, &one, Ww, N, Z, N, &zero, P, N));
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, N, &one, Ww, N, P, N, &zero, Z, N));
-      TRY(ortho_qr(st, N, r, Z, N, Qw, tau, &c->launches));
+    (*L)++;
+    // range finder (src/svd_clean.F90:183-255): Z = W_work P, q power iterations, each
+    // product re-orthonormalised by Householder QR
+    TRY(dgemm(st, 0, 0, N, r, N, 1.0, Ww, N, P, N, 0.0, Z, N, gws, L));
+    TRY(ortho_qr(st, N, r, Z, N, qrw, L));
+    for (int it = 0; it < q; it++) {
+      TRY(dgemm(st, 1, 0, N, r, N, 1.0, Ww, N, Z, N, 0.0, P, N, gws, L));
+      TRY(dgemm(st, 0, 0, N, r, N, 1.0, Ww, N, P, N, 0.0, Z, N, gws, L));
+      TRY(ortho_qr(st, N, r, Z, N, qrw, L));
     }
-    // Y = Z^T W_work (r x N, ld r); Y Y^T = UY D^2 UY^T
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, r, N, N, &one, Z, N, Ww, N, &zero, Y, r));
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, r, r, N, &one, Y, r, Y, r, &zero, G, r));
-    transpose_sym_kernel<<<nb((int64_t)r * r), 256, 0, st>>>(r, G, UY);  // UY (row-major) = sym(G)
-    TRY(sym_eig(st, r, UY, ev, ework, info, &c->launches));
-    reverse_eigvec_kernel<<<nb((int64_t)r * r), 256, 0, st>>>(r, UY, G);  // G <- UY col-major, descending
-    c->launches += 5;
-    SS_CUDA_TRY(cudaMemcpyAsync(hev.data(), ev, sizeof(double) * r, cudaMemcpyDeviceToHost, st));
-    int hinfo = 0;
-    SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
-    SS_CUDA_TRY(cudaStreamSynchronize(st));
-    if (hinfo) {
-      ss_set_error_msg("psd_clean: symmetric eigensolver did not converge (%d)", hinfo);
-      return SS_ERR_NUMERIC;
-    }
-    std::vector<double> inv(r);
-    for (int k = 0; k < r; k++) {
-      hD[k] = sqrt(std::max(hev[r - 1 - k], 0.0));
-      inv[k] = hD[k] > 0.0 ? 1.0 / hD[k] : 0.0;
-    }
-    SS_CUDA_TRY(cudaMemcpyAsync(Dd, inv.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
+    // SVD of Y = Z^T W_work (r x N) from Y Y^T = UY D^2 UY^T (src/svd.F90)
+    TRY(dgemm(st, 1, 0, r, N, N, 1.0, Z, N, Ww, N, 0.0, Y, r, gws, L));
+    TRY(dgemm(st, 0, 1, r, r, N, 1.0, Y, r, Y, r, 0.0, G, r, gws, L));
+    TRY(sym_eig(st, r, G, UYv, ev, eigw, derr, L));
+    svd_uy_kernel<<<nb((int64_t)r * r), 256, 0, st>>>(r, UYv, ev, UY, D, invD);
+    SS_CUDA_TRY(cudaGetLastError());
+    (*L)++;
     // Vt = D^-1 UY^T Y ; U = Z UY
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, r, N, r, &one, G, r, Y, r, &zero, Vt, r));
-    scale_rows_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(r, N, Vt, Dd);
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, r, r, &one, Z, N, G, r, &zero, U, N));
+    TRY(dgemm(st, 1, 0, r, N, r, 1.0, UY, r, Y, r, 0.0, Vt, r, gws, L));
+    scale_rows_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(r, N, Vt, invD);
+    SS_CUDA_TRY(cudaGetLastError());
+    TRY(dgemm(st, 0, 0, N, r, r, 1.0, Z, N, UY, r, 0.0, U, N, gws, L));
     sign_test_kernel<<<r, 256, 0, st>>>(N, r, U, Vt, rk);
-    c->launches += 2;
-    SS_CUDA_TRY(cudaMemcpyAsync(hR.data(), rk, sizeof(double) * r, cudaMemcpyDeviceToHost, st));
-    SS_CUDA_TRY(cudaStreamSynchronize(st));
-    // sign test (src/svd_clean.F90:286-296)
-    npass += r;
-    double dmax = 0.0;
-    std::vector<double> absD(r), negD(r);
-    int nneg = 0;
-    for (int k = 0; k < r; k++) {
-      if (hR[k] < 0.0) hD[k] = -hD[k];
-      if (fabs(hR[k]) < 0.99) {
-        hD[k] = 0.0;
-        npass--;
-      }
-      absD[k] = fabs(hD[k]);
-      negD[k] = hD[k] < 0.0 ? hD[k] : 0.0;
-      if (hD[k] < 0.0) nneg++;
-      dmax = std::max(dmax, fabs(hD[k]));
-    }
+    svd_sign_kernel<<<1, 1024, 0, st>>>(r, rk, D, absD, negD, dstats);
+    SS_CUDA_TRY(cudaGetLastError());
+    *L += 3;
     // W_work -= U |D| Vt ; W += U D_neg Vt   (src/svd_clean.F90:335-353)
-    SS_CUDA_TRY(cudaMemcpyAsync(Dd, absD.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
-    scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, Dd, Us);
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, N, r, &mone, Us, N, Vt, r, &one, Ww, N));
-    if (nneg) {
-      SS_CUDA_TRY(cudaMemcpyAsync(Dd, negD.data(), sizeof(double) * r, cudaMemcpyHostToDevice, st));
-      scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, Dd, Us);
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, N, r, &one, Us, N, Vt, r, &one, W, N));
-      c->launches++;
-      removed += nneg;
+    scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, absD, Us);
+    SS_CUDA_TRY(cudaGetLastError());
+    TRY(dgemm(st, 0, 0, N, N, r, -1.0, Us, N, Vt, r, 1.0, Ww, N, gws, L));
+    scale_cols_kernel<<<nb((int64_t)N * r), 256, 0, st>>>(N, r, U, negD, Us);
+    SS_CUDA_TRY(cudaGetLastError());
+    TRY(dgemm(st, 0, 0, N, N, r, 1.0, Us, N, Vt, r, 1.0, W, N, gws, L));
+    *L += 2;
+    SvdPassStats hs;
+    int herr = 0;
+    SS_CUDA_TRY(cudaMemcpyAsync(&hs, dstats, sizeof hs, cudaMemcpyDeviceToHost, st));
+    SS_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SS_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+      ss_set_error_msg("psd_clean: symmetric eigensolver %s (%d)", herr == 2 ? "grid barrier timed out" : "did not converge",
+                       herr);
+      return herr == 2 ? SS_ERR_TIMEOUT : SS_ERR_NUMERIC;
     }
-    c->launches++;
-    if (dmax < 1.e-12) npass = N;  // src/svd_clean.F90:359
+    npass += r - hs.nbad;
+    removed += hs.nneg;
+    if (hs.dmax < 1.e-12) npass = N;  // src/svd_clean.F90:359
     pass++;
     if (pass > 1000) {
       ss_set_error_msg("psd_clean: no convergence after 1000 passes");
@@ -331,7 +334,7 @@ int psd_clean(ss_ctx* c, double* moy_host, int layout, int rank, int oversample,
                                               (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
                                               (const int32_t*)c->d_ls.ptr, W, moy);
   SS_CUDA_TRY(cudaGetLastError());
-  c->launches++;
+  (*L)++;
   SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));
   SS_CUDA_TRY(cudaStreamSynchronize(st));
   if (n_removed) *n_removed = removed;
@@ -352,21 +355,15 @@ __global__ void gather_canonical_kernel(int64_t nint, int layout, int n, int64_t
     moy[q] = W[ss_pair_index(i, k) + ss_pair_index(j, l) * N];
 }
 
-__global__ void copy_rowmajor_kernel(int64_t NN, const double* __restrict__ in, double* __restrict__ out) {
+// columns of V scaled by min(lambda, 0) (the negative eigencomponents) and their count
+__global__ void neg_scale_kernel(int N, const double* __restrict__ V, const double* __restrict__ ev,
+                                 double* __restrict__ Vs, int* __restrict__ nneg) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e < NN) out[e] = in[e];  // W is symmetric: column-major == row-major
-}
-
-// V (row-major eigenvectors, N x N) columns 0..nneg-1 scaled by the eigenvalues -> Vs col-major,
-// Vc col-major copy (for W -= Vs Vc^T)
-__global__ void neg_components_kernel(int N, int nneg, const double* __restrict__ V, const double* __restrict__ ev,
-                                      double* __restrict__ Vs, double* __restrict__ Vc) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= (int64_t)N * nneg) return;
-  const int row = (int)(e % N), col = (int)(e / N);
-  const double v = V[(size_t)row * N + col];
-  Vc[e] = v;
-  Vs[e] = v * ev[col];
+  if (e >= (int64_t)N * N) return;
+  const int col = (int)(e / N);
+  const double l = ev[col];
+  Vs[e] = l < 0.0 ? V[e] * l : 0.0;
+  if (e % N == 0 && l < 0.0) atomicAdd(nneg, 1);
 }
 
 // Remove the negative eigencomponents exactly (src/davidson_clean.F90:30-116, the path the
@@ -376,61 +373,55 @@ __global__ void neg_components_kernel(int N, int nneg, const double* __restrict_
 int psd_project(ss_ctx* c, double* moy_host, int layout, int* n_removed) {
   const int n = c->n;
   const int64_t N64 = layout == SS_LAYOUT_REF_N2 ? (int64_t)n * n : (int64_t)n * (n + 1) / 2;
-  if (N64 > 1024) {
-    ss_set_error_msg("psd_project: matrix dimension %lld above the 1024 of the device eigensolver",
+  if (N64 > 2048) {
+    ss_set_error_msg("psd_project: matrix dimension %lld above the 2048 of the dense device eigensolver",
                      (long long)N64);
     return SS_ERR_UNSUPPORTED;
   }
   const int N = (int)N64;
-  cublasHandle_t hb;
-  TRY(get_cublas(c, &hb));
   void* p;
-  double *W, *A, *ev, *ework, *Vs, *Vc, *moy;
-  int* info;
+  double *W, *V, *ev, *Vs, *moy, *eigw, *gws;
   const size_t NN = (size_t)N * N;
   TRY(pool_get(c, "pj_W", sizeof(double) * NN, &p)); W = (double*)p;
-  TRY(pool_get(c, "pj_A", sizeof(double) * NN, &p)); A = (double*)p;
+  TRY(pool_get(c, "pj_V", sizeof(double) * NN, &p)); V = (double*)p;
   TRY(pool_get(c, "pj_ev", sizeof(double) * N, &p)); ev = (double*)p;
-  TRY(pool_get(c, "pj_ework", sizeof(double) * 2 * N, &p)); ework = (double*)p;
   TRY(pool_get(c, "pj_Vs", sizeof(double) * NN, &p)); Vs = (double*)p;
-  TRY(pool_get(c, "pj_Vc", sizeof(double) * NN, &p)); Vc = (double*)p;
   TRY(pool_get(c, "pj_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
-  TRY(pool_get(c, "pj_info", sizeof(int), &p)); info = (int*)p;
+  TRY(pool_get(c, "pj_eig", sizeof(double) * std::max<size_t>(sym_eig_ws(N), 1), &p)); eigw = (double*)p;
+  TRY(pool_get(c, "pj_gws", sizeof(double) * std::max<size_t>(dgemm_ws(N, N, N), 1), &p)); gws = (double*)p;
+  TRY(pool_get(c, "pj_ctl", 64, &p));
+  int* derr = (int*)p;
+  int* dneg = derr + 1;
+  int64_t* L = &c->launches;
   cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemsetAsync(derr, 0, 2 * sizeof(int), st));
   SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
   SS_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double) * NN, st));
   scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
                                                (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
                                                (const int32_t*)c->d_ls.ptr, moy, W);
-  copy_rowmajor_kernel<<<nb((int64_t)NN), 256, 0, st>>>((int64_t)NN, W, A);
   SS_CUDA_TRY(cudaGetLastError());
-  c->launches += 2;
-  TRY(sym_eig(st, N, A, ev, ework, info, &c->launches));
-  std::vector<double> hev(N);
-  int hinfo = 0;
-  SS_CUDA_TRY(cudaMemcpyAsync(hev.data(), ev, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
-  SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
-  SS_CUDA_TRY(cudaStreamSynchronize(st));
-  if (hinfo) {
-    ss_set_error_msg("psd_project: symmetric eigensolver did not converge (%d)", hinfo);
-    return SS_ERR_NUMERIC;
-  }
-  int nneg = 0;
-  while (nneg < N && hev[nneg] < 0.0) nneg++;  // ascending order
-  if (nneg) {
-    neg_components_kernel<<<nb((int64_t)N * nneg), 256, 0, st>>>(N, nneg, A, ev, Vs, Vc);
-    const double mone = -1.0, one = 1.0;
-    CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, N, N, nneg, &mone, Vs, N, Vc, N, &one, W, N));
-    c->launches += 2;
-  }
+  (*L)++;
+  TRY(sym_eig(st, N, W, V, ev, eigw, derr, L));
+  neg_scale_kernel<<<nb((int64_t)NN), 256, 0, st>>>(N, V, ev, Vs, dneg);
+  SS_CUDA_TRY(cudaGetLastError());
+  (*L)++;
+  TRY(dgemm(st, 0, 1, N, N, N, -1.0, Vs, N, V, N, 1.0, W, N, gws, L));
   gather_canonical_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
                                                         (const int32_t*)c->d_js.ptr, (const int32_t*)c->d_ks.ptr,
                                                         (const int32_t*)c->d_ls.ptr, W, moy);
   SS_CUDA_TRY(cudaGetLastError());
-  c->launches++;
+  (*L)++;
+  int hctl[2] = {0, 0};
+  SS_CUDA_TRY(cudaMemcpyAsync(hctl, derr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
   SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));
   SS_CUDA_TRY(cudaStreamSynchronize(st));
-  if (n_removed) *n_removed = nneg;
+  if (hctl[0]) {
+    ss_set_error_msg("psd_project: symmetric eigensolver %s (%d)",
+                     hctl[0] == 2 ? "grid barrier timed out" : "did not converge", hctl[0]);
+    return hctl[0] == 2 ? SS_ERR_TIMEOUT : SS_ERR_NUMERIC;
+  }
+  if (n_removed) *n_removed = hctl[1];
   return SS_OK;
 }
 
@@ -468,6 +459,23 @@ __global__ void col_norms_kernel(int N, int m, const double* __restrict__ X, dou
   }
 }
 
+// largest of the m correction norms (one warp)
+__global__ void max_norm_kernel(int m, const double* __restrict__ nrm, double* __restrict__ out) {
+  double v = 0.0;
+  for (int j = threadIdx.x; j < m; j += 32) v = fmax(v, nrm[j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if (threadIdx.x == 0) *out = v;
+}
+
+// symmetrised copy: out = (in + in^T) / 2, k x k col-major
+__global__ void sym_copy_kernel(int k, const double* __restrict__ in, double* __restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)k * k) return;
+  const int i = (int)(e % k), j = (int)(e / k);
+  out[e] = 0.5 * (in[i + (size_t)j * k] + in[j + (size_t)i * k]);
+}
+
 int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, int max_iter, double* evals,
              double* evecs) {
   const int n = c->n;
@@ -479,35 +487,37 @@ int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, i
   const int N = (int)N64;
   const int nmax = std::max(2, std::min(10, N / m));  // src/davidson.F90:21
   const int kmax = nmax * m;
-  if (kmax > N) {
-    ss_set_error_msg("davidson: subspace %d larger than the matrix %d", kmax, N);
+  if (kmax > N || kmax > 2048) {
+    ss_set_error_msg("davidson: subspace %d larger than the matrix %d (or 2048)", kmax, N);
     return SS_ERR_ARG;
   }
-  cublasHandle_t hb;
-  TRY(get_cublas(c, &hb));
   void* p;
-  double *H, *Hd, *U, *WU, *S, *Sa, *ev, *ework, *X, *WX, *Cc, *E, *nrm, *tmp, *moy, *Qw, *tau;
-  int* info;
-  const size_t NN = (size_t)N * N, Nk = (size_t)N * kmax;
+  double *H, *Hd, *U, *WU, *S, *Sa, *Vk, *ev, *X, *WX, *Cc, *nrm, *tmp, *moy, *qrw, *eigw, *gws, *ctl;
+  const size_t NN = (size_t)N * N, Nk = (size_t)N * kmax, kk2 = (size_t)kmax * kmax;
+  const size_t gsz = std::max({dgemm_ws(N, m, N), dgemm_ws(kmax, kmax, N), dgemm_ws(N, m, kmax),
+                               dgemm_ws(kmax, m, N), (size_t)1});
   TRY(pool_get(c, "dv_H", sizeof(double) * NN, &p)); H = (double*)p;
   TRY(pool_get(c, "dv_Hd", sizeof(double) * N, &p)); Hd = (double*)p;
   TRY(pool_get(c, "dv_U", sizeof(double) * Nk, &p)); U = (double*)p;
   TRY(pool_get(c, "dv_WU", sizeof(double) * Nk, &p)); WU = (double*)p;
-  TRY(pool_get(c, "dv_S", sizeof(double) * kmax * kmax, &p)); S = (double*)p;
-  TRY(pool_get(c, "dv_Sa", sizeof(double) * kmax * kmax, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dv_S", sizeof(double) * kk2, &p)); S = (double*)p;
+  TRY(pool_get(c, "dv_Sa", sizeof(double) * kk2, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dv_Vk", sizeof(double) * kk2, &p)); Vk = (double*)p;
   TRY(pool_get(c, "dv_ev", sizeof(double) * kmax, &p)); ev = (double*)p;
-  TRY(pool_get(c, "dv_ework", sizeof(double) * 2 * kmax, &p)); ework = (double*)p;
   TRY(pool_get(c, "dv_X", sizeof(double) * (size_t)N * m, &p)); X = (double*)p;
   TRY(pool_get(c, "dv_WX", sizeof(double) * (size_t)N * m, &p)); WX = (double*)p;
   TRY(pool_get(c, "dv_C", sizeof(double) * (size_t)N * m, &p)); Cc = (double*)p;
-  TRY(pool_get(c, "dv_E", sizeof(double) * m, &p)); E = (double*)p;
   TRY(pool_get(c, "dv_nrm", sizeof(double) * m, &p)); nrm = (double*)p;
   TRY(pool_get(c, "dv_tmp", sizeof(double) * (size_t)kmax * m, &p)); tmp = (double*)p;
   TRY(pool_get(c, "dv_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
-  TRY(pool_get(c, "dv_Qw", sizeof(double) * Nk, &p)); Qw = (double*)p;
-  TRY(pool_get(c, "dv_tau", sizeof(double) * kmax, &p)); tau = (double*)p;
-  TRY(pool_get(c, "dv_info", sizeof(int), &p)); info = (int*)p;
+  TRY(pool_get(c, "dv_qr", sizeof(double) * ortho_qr_ws(N, m), &p)); qrw = (double*)p;
+  TRY(pool_get(c, "dv_eig", sizeof(double) * std::max<size_t>(sym_eig_ws(kmax), 1), &p)); eigw = (double*)p;
+  TRY(pool_get(c, "dv_gws", sizeof(double) * gsz, &p)); gws = (double*)p;
+  TRY(pool_get(c, "dv_ctl", 64, &p)); ctl = (double*)p;  // [0] max correction norm, [1] error flag
+  int* derr = (int*)(ctl + 1);
+  int64_t* L = &c->launches;
   cudaStream_t st = c->stream;
+  SS_CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), st));
   SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
   SS_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * NN, st));
   scatter_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, (const int32_t*)c->d_is.ptr,
@@ -516,74 +526,64 @@ int davidson(ss_ctx* c, const double* moy_host, int layout, int m, double tol, i
   diag_kernel<<<(N + 255) / 256, 256, 0, st>>>(N, H, Hd);
   // random normalised start vectors (src/davidson.F90:26-37), orthonormalised
   gaussian_matrix_kernel<<<m, 256, 0, st>>>(1, 0x44415649u, N, m, U);
-  TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
-  c->launches += 3;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
-  std::vector<double> hE(m), hn(m);
+  SS_CUDA_TRY(cudaGetLastError());
+  *L += 3;
+  TRY(ortho_qr(st, N, m, U, N, qrw, L));
+  std::vector<double> hE(m);
+  double hmax = 0.0;
   bool converged = false;
   int total = 0;
   while (!converged && total < max_iter) {
     for (int iter = 1; iter <= nmax - 1 && !converged && total < max_iter; iter++, total++) {
       const int shift = m * (iter - 1);
       // W(:, shift:shift+m) = H U(:, shift:shift+m)
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, N, &one, H, N, U + (size_t)shift * N, N, &zero,
-                             WU + (size_t)shift * N, N));
+      TRY(dgemm(st, 0, 0, N, m, N, 1.0, H, N, U + (size_t)shift * N, N, 0.0, WU + (size_t)shift * N, N, gws, L));
       const int k = shift + m;
-      // projected matrix S = U^T W (k x k), symmetrised, eigen-decomposed
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, k, N, &one, U, N, WU, N, &zero, S, k));
-      transpose_sym_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
-      TRY(sym_eig(st, k, Sa, ev, ework, info, &c->launches));
-      // lowest m Ritz vectors: columns 0..m-1 of Sa (row-major) -> tmp (k x m col-major)
-      c->launches += 1;
-      // copy eigenvector columns: Sa row-major (row i, col j) at i*k + j; tmp col-major (i, j) at i + j*k
-      std::vector<double> hv((size_t)k * k);
-      SS_CUDA_TRY(cudaMemcpyAsync(hv.data(), Sa, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
-      SS_CUDA_TRY(cudaMemcpyAsync(hE.data(), ev, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
-      int hinfo = 0;
-      SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
-      SS_CUDA_TRY(cudaStreamSynchronize(st));
-      if (hinfo) {
-        ss_set_error_msg("davidson: projected eigenproblem did not converge");
-        return SS_ERR_NUMERIC;
-      }
-      std::vector<double> ht((size_t)k * m);
-      for (int j = 0; j < m; j++)
-        for (int i = 0; i < k; i++) ht[i + (size_t)j * k] = hv[(size_t)i * k + j];
-      SS_CUDA_TRY(cudaMemcpyAsync(tmp, ht.data(), sizeof(double) * k * m, cudaMemcpyHostToDevice, st));
-      SS_CUDA_TRY(cudaMemcpyAsync(E, hE.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-      // X = U v, WX = W v (src/davidson.F90:118-126)
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, U, N, tmp, k, &zero, X, N));
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, WU, N, tmp, k, &zero, WX, N));
-      davidson_correction<<<nb((int64_t)N * m), 256, 0, st>>>(N, m, X, WX, E, Hd, Cc);
+      // projected matrix S = U^T W (k x k), symmetrised, eigen-decomposed (ascending)
+      TRY(dgemm(st, 1, 0, k, k, N, 1.0, U, N, WU, N, 0.0, S, k, gws, L));
+      sym_copy_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
+      SS_CUDA_TRY(cudaGetLastError());
+      (*L)++;
+      TRY(sym_eig(st, k, Sa, Vk, ev, eigw, derr, L));
+      // Ritz vectors X = U v, W X = W v of the lowest m (src/davidson.F90:118-126)
+      TRY(dgemm(st, 0, 0, N, m, k, 1.0, U, N, Vk, k, 0.0, X, N, gws, L));
+      TRY(dgemm(st, 0, 0, N, m, k, 1.0, WU, N, Vk, k, 0.0, WX, N, gws, L));
+      davidson_correction<<<nb((int64_t)N * m), 256, 0, st>>>(N, m, X, WX, ev, Hd, Cc);
       col_norms_kernel<<<m, 256, 0, st>>>(N, m, Cc, nrm);
-      c->launches += 2;
-      SS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+      max_norm_kernel<<<1, 32, 0, st>>>(m, nrm, ctl);
+      SS_CUDA_TRY(cudaGetLastError());
+      *L += 3;
+      int herr = 0;
+      SS_CUDA_TRY(cudaMemcpyAsync(&hmax, ctl, sizeof(double), cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
       SS_CUDA_TRY(cudaStreamSynchronize(st));
-      double mx = 0.0;
-      for (double v : hn) mx = std::max(mx, v);
-      converged = mx < tol;  // src/davidson.F90:143
+      if (herr) {
+        ss_set_error_msg("davidson: projected eigenproblem %s", herr == 2 ? "timed out" : "did not converge");
+        return herr == 2 ? SS_ERR_TIMEOUT : SS_ERR_NUMERIC;
+      }
+      converged = hmax < tol;  // src/davidson.F90:143
       if (converged || iter == nmax - 1) break;
       // new block: corrections orthogonalised against U (twice) and among themselves
       double* Un = U + (size_t)k * N;
       SS_CUDA_TRY(cudaMemcpyAsync(Un, Cc, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, st));
       for (int rep = 0; rep < 2; rep++) {
-        CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, m, N, &one, U, N, Un, N, &zero, tmp, k));
-        CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &mone, U, N, tmp, k, &one, Un, N));
+        TRY(dgemm(st, 1, 0, k, m, N, 1.0, U, N, Un, N, 0.0, tmp, k, gws, L));
+        TRY(dgemm(st, 0, 0, N, m, k, -1.0, U, N, tmp, k, 1.0, Un, N, gws, L));
       }
-      TRY(ortho_qr(st, N, m, Un, N, Qw, tau, &c->launches));
+      TRY(ortho_qr(st, N, m, Un, N, qrw, L));
     }
     // restart with the current Ritz vectors (src/davidson.F90:151-155)
     SS_CUDA_TRY(cudaMemcpyAsync(U, X, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, st));
-    TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+    TRY(ortho_qr(st, N, m, U, N, qrw, L));
   }
   if (!converged) {
-    ss_set_error_msg("davidson: not converged after %d iterations (largest correction %g)", max_iter,
-                     *std::max_element(hn.begin(), hn.end()));
+    ss_set_error_msg("davidson: not converged after %d iterations (largest correction %g)", max_iter, hmax);
     return SS_ERR_NUMERIC;
   }
-  if (evals) memcpy(evals, hE.data(), sizeof(double) * m);
+  SS_CUDA_TRY(cudaMemcpyAsync(hE.data(), ev, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
   if (evecs) SS_CUDA_TRY(cudaMemcpyAsync(evecs, X, sizeof(double) * N * m, cudaMemcpyDeviceToHost, st));
   SS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (evals) memcpy(evals, hE.data(), sizeof(double) * m);
   return SS_OK;
 }
 
@@ -659,14 +659,6 @@ __global__ void __launch_bounds__(256) op_apply_kernel(int layout, int n, int N,
   }
 }
 
-// lowest m eigenvectors of the k x k projected matrix (row-major, eigenvectors as columns)
-// into V (k x m column-major)
-__global__ void ritz_cols_kernel(int k, int m, const double* __restrict__ A, double* __restrict__ V) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= (int64_t)k * m) return;
-  const int i = (int)(e % k), j = (int)(e / k);
-  V[e] = A[(size_t)i * k + j];
-}
 
 // residuals R_j = E_j X_j - (H X)_j (src/davidson_clean.F90:277-283)
 __global__ void residual_kernel(int N, int m, const double* __restrict__ X, const double* __restrict__ WX,
@@ -709,15 +701,14 @@ static int op_apply(ss_ctx* c, int layout, int N, int m, const double* tri, cons
 // Gram-Schmidt passes against U, Householder QR of the block, then the pair once more (a block
 // whose residuals vanished comes back from the first QR with unit columns that need not be
 // orthogonal to U).
-static int orthonormalize_block(ss_ctx* c, cublasHandle_t hb, int N, int k, int b, const double* U, double* V,
-                                double* tmp, double* Qw, double* tau) {
-  const double one = 1.0, zero = 0.0, mone = -1.0;
+static int orthonormalize_block(ss_ctx* c, int N, int k, int b, const double* U, double* V, double* tmp,
+                                double* qrw, double* gws) {
   for (int round = 0; round < 2; round++) {
     for (int rep = 0; rep < 2 && k > 0; rep++) {
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, b, N, &one, U, N, V, N, &zero, tmp, k));
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, b, k, &mone, U, N, tmp, k, &one, V, N));
+      TRY(dgemm(c->stream, 1, 0, k, b, N, 1.0, U, N, V, N, 0.0, tmp, k, gws, &c->launches));
+      TRY(dgemm(c->stream, 0, 0, N, b, k, -1.0, U, N, tmp, k, 1.0, V, N, gws, &c->launches));
     }
-    TRY(ortho_qr(c->stream, N, b, V, N, Qw, tau, &c->launches));
+    TRY(ortho_qr(c->stream, N, b, V, N, qrw, &c->launches));
   }
   return SS_OK;
 }
@@ -759,34 +750,35 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
   double scale = 0.0;
   for (int64_t q = 0; q < c->nint; q++) scale = std::max(scale, fabs(moy_host[q]));
   const double neg_eps = 1e-13 * scale;
-  cublasHandle_t hb;
-  TRY(get_cublas(c, &hb));
   void* p;
-  double *tri, *U, *WU, *S, *Sa, *ev, *ework, *X, *WX, *R, *nrm, *tmp, *moy, *Qw, *tau;
-  int* info;
+  double *tri, *U, *WU, *S, *Sa, *Vk, *ev, *X, *WX, *R, *nrm, *tmp, *moy, *qrw, *eigw, *gws;
   const int64_t T = (int64_t)(n * (n + 1) / 2) * (n * (n + 1) / 2 + 1) / 2;
-  const size_t Nk = (size_t)N * kmax, Nm = (size_t)N * m;
+  const size_t Nk = (size_t)N * kmax, Nm = (size_t)N * m, kk2 = (size_t)kmax * kmax;
+  const size_t gsz = std::max({dgemm_ws(kmax, kmax, N), dgemm_ws(N, m, kmax), dgemm_ws(kmax, m, N), (size_t)1});
   TRY(pool_get(c, "dc_tri", sizeof(double) * T, &p)); tri = (double*)p;
   TRY(pool_get(c, "dc_U", sizeof(double) * Nk, &p)); U = (double*)p;
   TRY(pool_get(c, "dc_WU", sizeof(double) * Nk, &p)); WU = (double*)p;
-  TRY(pool_get(c, "dc_S", sizeof(double) * kmax * kmax, &p)); S = (double*)p;
-  TRY(pool_get(c, "dc_Sa", sizeof(double) * kmax * kmax, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dc_S", sizeof(double) * kk2, &p)); S = (double*)p;
+  TRY(pool_get(c, "dc_Sa", sizeof(double) * kk2, &p)); Sa = (double*)p;
+  TRY(pool_get(c, "dc_Vk", sizeof(double) * kk2, &p)); Vk = (double*)p;
   TRY(pool_get(c, "dc_ev", sizeof(double) * kmax, &p)); ev = (double*)p;
-  TRY(pool_get(c, "dc_ework", sizeof(double) * 2 * kmax, &p)); ework = (double*)p;
   TRY(pool_get(c, "dc_X", sizeof(double) * Nm, &p)); X = (double*)p;
   TRY(pool_get(c, "dc_WX", sizeof(double) * Nm, &p)); WX = (double*)p;
   TRY(pool_get(c, "dc_R", sizeof(double) * Nm, &p)); R = (double*)p;
   TRY(pool_get(c, "dc_nrm", sizeof(double) * m, &p)); nrm = (double*)p;
   TRY(pool_get(c, "dc_tmp", sizeof(double) * (size_t)kmax * m, &p)); tmp = (double*)p;
   TRY(pool_get(c, "dc_moy", sizeof(double) * c->nint, &p)); moy = (double*)p;
-  TRY(pool_get(c, "dc_Qw", sizeof(double) * Nm, &p)); Qw = (double*)p;
-  TRY(pool_get(c, "dc_tau", sizeof(double) * m, &p)); tau = (double*)p;
-  TRY(pool_get(c, "dc_info", sizeof(int), &p)); info = (int*)p;
+  TRY(pool_get(c, "dc_qr", sizeof(double) * ortho_qr_ws(N, m), &p)); qrw = (double*)p;
+  TRY(pool_get(c, "dc_eig", sizeof(double) * std::max<size_t>(sym_eig_ws(kmax), 1), &p)); eigw = (double*)p;
+  TRY(pool_get(c, "dc_gws", sizeof(double) * gsz, &p)); gws = (double*)p;
+  TRY(pool_get(c, "dc_ctl", 64, &p));
+  int* derr = (int*)p;
+  int64_t* L = &c->launches;
   cudaStream_t st = c->stream;
   const int32_t *d_is = (const int32_t*)c->d_is.ptr, *d_js = (const int32_t*)c->d_js.ptr,
                 *d_ks = (const int32_t*)c->d_ks.ptr, *d_ls = (const int32_t*)c->d_ls.ptr;
+  SS_CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), st));
   SS_CUDA_TRY(cudaMemcpyAsync(moy, moy_host, sizeof(double) * c->nint, cudaMemcpyHostToDevice, st));
-  const double one = 1.0, zero = 0.0;
   std::vector<double> hE(m), hn(m);
   int removed = 0, total = 0;
   for (int pass = 0;; pass++) {
@@ -794,8 +786,8 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
     tri_fill_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, d_is, d_js, d_ks, d_ls, moy, tri);
     // normalised Gaussian start vectors (src/davidson_clean.F90:137-149), orthonormalised
     gaussian_matrix_kernel<<<m, 256, 0, st>>>(1, 0x44434c00u + (uint32_t)pass, N, m, U);
-    c->launches += 2;
-    TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+    *L += 2;
+    TRY(ortho_qr(st, N, m, U, N, qrw, L));
     TRY(op_apply(c, layout, N, m, tri, U, WU));
     int k = m;
     for (;;) {
@@ -805,24 +797,23 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
         return SS_ERR_NUMERIC;
       }
       // Rayleigh-Ritz on span(U): S = U^T H U, lowest m eigenpairs
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, k, k, N, &one, U, N, WU, N, &zero, S, k));
-      transpose_sym_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
-      c->launches++;
-      TRY(sym_eig(st, k, Sa, ev, ework, info, &c->launches));
-      ritz_cols_kernel<<<nb((int64_t)k * m), 256, 0, st>>>(k, m, Sa, tmp);
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, U, N, tmp, k, &zero, X, N));
-      CUBLAS_TRY(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, N, m, k, &one, WU, N, tmp, k, &zero, WX, N));
+      TRY(dgemm(st, 1, 0, k, k, N, 1.0, U, N, WU, N, 0.0, S, k, gws, L));
+      sym_copy_kernel<<<nb((int64_t)k * k), 256, 0, st>>>(k, S, Sa);
+      (*L)++;
+      TRY(sym_eig(st, k, Sa, Vk, ev, eigw, derr, L));
+      TRY(dgemm(st, 0, 0, N, m, k, 1.0, U, N, Vk, k, 0.0, X, N, gws, L));
+      TRY(dgemm(st, 0, 0, N, m, k, 1.0, WU, N, Vk, k, 0.0, WX, N, gws, L));
       residual_kernel<<<nb((int64_t)N * m), 256, 0, st>>>(N, m, X, WX, ev, R);
       col_norms_kernel<<<m, 256, 0, st>>>(N, m, R, nrm);
-      c->launches += 3;
-      int hinfo = 0;
+      *L += 2;
+      int herr = 0;
       SS_CUDA_TRY(cudaMemcpyAsync(hE.data(), ev, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
       SS_CUDA_TRY(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
-      SS_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SS_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
       SS_CUDA_TRY(cudaStreamSynchronize(st));
-      if (hinfo) {
-        ss_set_error_msg("davidson_clean: projected eigenproblem did not converge");
-        return SS_ERR_NUMERIC;
+      if (herr) {
+        ss_set_error_msg("davidson_clean: projected eigenproblem %s", herr == 2 ? "timed out" : "did not converge");
+        return herr == 2 ? SS_ERR_TIMEOUT : SS_ERR_NUMERIC;
       }
       double rmax = 0.0;
       for (int j = 0; j < m; j++)
@@ -830,14 +821,14 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
       if (rmax < tol || k == N) break;
       if (k + m > kmax) {  // restart from the Ritz vectors (src/davidson_clean.F90:293-299)
         SS_CUDA_TRY(cudaMemcpyAsync(U, X, sizeof(double) * Nm, cudaMemcpyDeviceToDevice, st));
-        TRY(ortho_qr(st, N, m, U, N, Qw, tau, &c->launches));
+        TRY(ortho_qr(st, N, m, U, N, qrw, L));
         TRY(op_apply(c, layout, N, m, tri, U, WU));
         k = m;
         continue;
       }
       double* Un = U + (size_t)k * N;
       SS_CUDA_TRY(cudaMemcpyAsync(Un, R, sizeof(double) * Nm, cudaMemcpyDeviceToDevice, st));
-      TRY(orthonormalize_block(c, hb, N, k, m, U, Un, tmp, Qw, tau));
+      TRY(orthonormalize_block(c, N, k, m, U, Un, tmp, qrw, gws));
       TRY(op_apply(c, layout, N, m, tri, Un, WU + (size_t)k * N));
       k += m;
     }
@@ -846,7 +837,7 @@ int davidson_clean(ss_ctx* c, double* moy_host, int layout, int m, int nmax, dou
     if (nneg == 0) break;
     deflate_kernel<<<nb(c->nint), 256, 0, st>>>(c->nint, layout, n, N, d_is, d_js, d_ks, d_ls, nneg, ev, X, moy);
     SS_CUDA_TRY(cudaGetLastError());
-    c->launches++;
+    (*L)++;
     removed += nneg;
   }
   SS_CUDA_TRY(cudaMemcpyAsync(moy_host, moy, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, st));

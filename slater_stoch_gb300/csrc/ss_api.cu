@@ -455,7 +455,6 @@ void ss_destroy(ss_ctx* c) {
                     &c->d_mono_status};
   for (DevBuf* b : bufs) dev_free(c, *b);
   for (auto& kv : c->pool) dev_free(c, kv.second);
-  destroy_cublas(c->cublas_handle);
   for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
     if (c->eri_stream[s]) cudaStreamDestroy(c->eri_stream[s]);
     if (c->eri_join[s]) cudaEventDestroy(c->eri_join[s]);

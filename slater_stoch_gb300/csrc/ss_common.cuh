@@ -34,12 +34,15 @@ constexpr int SLOT_SPLIT_BITS = 7;
 __host__ __device__ inline int64_t slot_offset(int64_t code) { return code >> SLOT_SPLIT_BITS; }
 __host__ __device__ inline int slot_split(int64_t code) { return (int)(code & ((1 << SLOT_SPLIT_BITS) - 1)); }
 // Mixed precision: a kept primitive quartet whose Schwarz bound S_P S_Q is below
-// PRIM_FP32_EPS * sqrt((ik|ik)(jl|jl)) is evaluated in FP32.  Its value is off by about
-// kappa * 6e-8 * S_P S_Q (kappa the cancellation amplification of its evaluation), or by its
-// whole value when its FP32 prefactor K_AB c_P c_Q underflows -- terms of ~1e-40 then.  Summed
-// over a quartet's tier the difference from FP64 was measured below 1.1e-17 of the Schwarz bound
-// (20-Gaussian fits), five orders below the 1e-12 accuracy the ERIs are held to.
-constexpr double PRIM_FP32_EPS = 1e-13;
+// PRIM_FP32_EPS * sqrt((ik|ik)(jl|jl)) is evaluated in FP32 (the default of ss_set_eri_tiers).
+// Its value is off by about kappa * 6e-8 * S_P S_Q (kappa the cancellation amplification of its
+// evaluation), or by its whole value when its FP32 prefactor K_AB c_P c_Q underflows -- terms of
+// ~1e-40 then.  Summed over a quartet's tier the difference from FP64 was measured at 1.8e-15 of
+// the Schwarz bound (20-Gaussian fits, host build of the kernel arithmetic), and on the device
+// the largest deviation from the oracle over a stratified sample of the 26-function H2O basis
+// was 6.4e-3 of the 1e-12 gate (1.1e-3 with a 1e-13 threshold).  The tier takes 40 % of the
+// primitive quartets there (28 % at 1e-13), leaving 30 % in FP64.
+constexpr double PRIM_FP32_EPS = 1e-11;
 
 // One primitive pair of a function pair (i,k): the Gaussian product of
 // g_gauss(m1,i) and g_gauss(m2,k) (src/gaussian_product.F90:1-33), padded to 128 bytes.

@@ -105,7 +105,6 @@ struct ss_ctx {
   ss::DevBuf d_scratch_a, d_scratch_b, d_scratch_c, d_scratch_d;
   // named device buffers of the MC and cleanup stages
   std::map<std::string, ss::DevBuf> pool;
-  void* cublas_handle = nullptr;  // cublasHandle_t of the cleanup stage
   int mc_blocks_done = 0;
   double mc_max_sigma = 0.0;
 };
@@ -118,5 +117,4 @@ int ensure_precond(ss_ctx* c);
 // named pool buffer of at least `bytes`; *out receives the device pointer
 int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out);
 int ensure_gauss(ss_ctx* c);
-void destroy_cublas(void* h);
 }  // namespace ss

@@ -6,7 +6,6 @@ the device, without the device's screening and FP32 tier.
 Gate (the GPU parity gate): |host - oracle| <= 1e-12 |oracle| + 1e-12 sqrt((ik|ik)(jl|jl)).
 The light-ket instances, the full-L instances and the full-L instances with every quartet
 evaluated as (jl|ik) agree with each other within the same gate."""
-import ctypes as C
 import shutil
 import subprocess
 from pathlib import Path
@@ -14,40 +13,26 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import eri_host
 from slater_stoch_gb300 import basis, configs
 
 HERE = Path(__file__).resolve().parent
-PRIM_FP32_EPS = 1e-13  # the kernel's threshold of the FP32 tier (csrc/ss_common.cuh)
+PRIM_FP32_EPS = 1e-11  # the kernel's default threshold of the FP32 tier (csrc/ss_common.cuh)
 CSRC = HERE.parent / "slater_stoch_gb300" / "csrc"
 
 
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
-    gxx, nvcc = shutil.which("g++"), shutil.which("nvcc")
-    if gxx is None or nvcc is None:
+    if not eri_host.available():
         pytest.skip("g++ or the CUDA headers not available")
-    cuda_inc = Path(nvcc).resolve().parent.parent / "include"
-    out = tmp_path_factory.mktemp("eri") / "liberi_host.so"
-    subprocess.run([gxx, "-O1", "-std=c++17", "-ffp-contract=off", "-Wno-unknown-pragmas", "-shared", "-fPIC",
-                    f"-I{cuda_inc}", f"-I{CSRC}", str(HERE / "eri_host_shim.cpp"), "-o", str(out)], check=True)
-    L = C.CDLL(str(out))
-    f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
-    i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
-    L.ss_host_eri.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
-                              i32p, i32p, i32p, i32p, C.c_int, C.c_int, f64p, i32p]
-    L.ss_host_eri.restype = C.c_int
-    return L
+    return eri_host.load(eri_host.build(tmp_path_factory.mktemp("eri")))
 
 
 def _host_eri(lib, b, q, mode=0, fold=1):
-    arrs = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
-            np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
-            np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
-            np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
     qq = [np.ascontiguousarray(x, np.int32) for x in q]
     out = np.zeros(len(qq[0]))
     lk = np.zeros(len(qq[0]), np.int32)
-    rc = lib.ss_host_eri(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq, mode, fold, out, lk)
+    rc = lib.ss_host_eri(int(b.n), int(b.ld), *eri_host.basis_arrays(b), len(qq[0]), *qq, mode, fold, out, lk)
     assert rc == 0
     return out, lk
 
@@ -101,33 +86,26 @@ def test_folding_is_exact(lib):
 
 
 def _fp32_error(lib, b, q, pre):
-    arrs = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
-            np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
-            np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
-            np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
     qq = [np.ascontiguousarray(x, np.int32) for x in q]
     out = np.zeros(7)
-    f64p = np.ctypeslib.ndpointer(np.float64, flags="C")
-    i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
-    lib.ss_host_fp32_error.argtypes = [C.c_int, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, f64p, f64p, C.c_int64,
-                                       i32p, i32p, i32p, i32p, f64p, C.c_double, f64p]
-    assert lib.ss_host_fp32_error(int(b.n), int(b.ld), *arrs, len(qq[0]), *qq,
+    assert lib.ss_host_fp32_error(int(b.n), int(b.ld), *eri_host.basis_arrays(b), len(qq[0]), *qq,
                                   np.ascontiguousarray(pre, np.float64), PRIM_FP32_EPS, out) == 0
     return {"n_tier": int(out[3]), "signed": out[4], "abs": out[5], "acc": out[6]}
 
 
 def test_fp32_tier_error_is_negligible(lib, h2o26):
-    """The FP32 tier (primitive quartets below 1e-13 of the Schwarz bound sqrt((ik|ik)(jl|jl)),
+    """The FP32 tier (primitive quartets below 1e-11 of the Schwarz bound sqrt((ik|ik)(jl|jl)),
     evaluated as the kernel does: FP32 bra polynomials from the FP32 pair copies, ket polynomials
     rounded from FP64, K_AB c folded into the FP32 factor) changes each ERI by far less than the
-    1e-12 gate: the sum of |FP32 - FP64| over a quartet's tier stays below 1e-15 of its Schwarz
-    bound.  (A single primitive quartet can be off by its whole bound when its FP32 prefactor
-    underflows, but such terms are ~1e-40 in absolute size.)  Every quartet of the 26-function
-    basis at 3-Gaussian fits, and 10 quartets at the production 20-Gaussian fits."""
+    1e-12 gate: the sum of |FP32 - FP64| over a quartet's tier, and the rounding of the
+    per-thread FP32 running sums, stay below 2e-14 of its Schwarz bound (measured: 1.2e-15 and
+    5.0e-15 at 20-Gaussian fits).  (A single primitive quartet can be off by its whole bound when
+    its FP32 prefactor underflows, but such terms are ~1e-40 in absolute size.)  Every quartet of
+    the 26-function basis at 3-Gaussian fits, and 10 quartets at the production 20-Gaussian fits."""
     from oracle import binding as O
     b, q, pre, ref = h2o26
     e = _fp32_error(lib, b, q, pre)
-    assert e["n_tier"] > 0 and e["abs"] < 1e-15
+    assert e["n_tier"] > 0 and e["abs"] < 2e-14
     b20 = configs.h2o_26(ng0=20)
     q20 = np.array(basis.build_mapping(b20.n))
     sel = np.random.default_rng(11).choice(q20.shape[1], 10, replace=False)
@@ -141,8 +119,8 @@ def test_fp32_tier_error_is_negligible(lib, h2o26):
     for (i, k), v in zip(pairs, diag):
         pre20[i - 1, k - 1] = pre20[k - 1, i - 1] = v
     e20 = _fp32_error(lib, b20, [qs[r] for r in range(4)], pre20.reshape(-1, order="F"))
-    assert e20["n_tier"] > 100000 and e20["abs"] < 1e-15
-    assert e20["acc"] < 1e-15  # the per-thread FP32 running sums
+    assert e20["n_tier"] > 100000 and e20["abs"] < 2e-14
+    assert e20["acc"] < 2e-14  # the per-thread FP32 running sums
 
 
 def test_threshold_matches_the_kernel():

@@ -84,13 +84,13 @@ def h2o26_ng20(tmp_path_factory):
     return O, b, q, ob, pre, L, {}  # the last: oracle values by quartet index, shared by the cases
 
 
-@pytest.mark.parametrize("fp32_eps", [1e-13, 1e-11])
+@pytest.mark.parametrize("fp32_eps", [1e-11, 1e-13])
 def test_gauss_eri_h2o26_ng20_stratified(h2o26_ng20, fp32_eps):
     """All 61,776 ERIs of the benchmarked configuration computed on the device; compared with the
     oracle on the whole Schwarz diagonal (351 quartets (ik|ik)), a stratified sample of >= 40
     quartets from every kernel instance (L, LK, tc), and the 50 quartets whose kept primitive
     quartets go most to the FP32 tier.  Gate per quartet: 1e-12 |ERI| + 1e-12 sqrt((ik|ik)(jl|jl)).
-    Run at the default FP32-tier threshold (1e-13 of the Schwarz bound) and at 1e-11."""
+    Run at the default FP32-tier threshold (1e-11 of the Schwarz bound) and at 1e-13."""
     import eri_host
     O, b, q, ob, pre, L, memo = h2o26_ng20
     counts, cls = eri_host.tier_counts(L, b, q, pre, 1e-18, fp32_eps)
