@@ -169,6 +169,25 @@ def run_reference(args):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def serving_run(rate: float, duration: float, large: str, max_running: int, seed: int = 1) -> dict:
+    """Open-loop Poisson serving run (slater_stoch_gb300.serving): requests arrive at `rate`
+    per second for `duration` seconds, each a small random system (1-2 atoms of the random-
+    molecule rules, 4-22 STOs) or with probability 0.05 the `large` system, with error-bar
+    targets log-uniform in [1e-7, 1e-5] Ha; admitted within a 150 GB ERI budget and
+    `max_running` concurrent jobs, each retired at its target."""
+    from slater_stoch_gb300 import configs, serving
+    big = getattr(configs, large)(ng0=20)
+    reqs = serving.make_requests(seed, rate, duration, large=big)
+    t = time.perf_counter()
+    rep = serving.serve(reqs, max_running=max_running)
+    out = rep.summary()
+    out.update({"rate_per_s": rate, "duration_s": duration, "large_system": large,
+                "requests": len(reqs), "max_running": max_running,
+                "sizes_nbasis": [int(min(r.basis.n for r in reqs)), int(max(r.basis.n for r in reqs))],
+                "elapsed_s": time.perf_counter() - t})
+    return out
+
+
 def fp64_peak_tflops(torch):
     n = 4096
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
@@ -195,11 +214,23 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="h2o_26", choices=["h2o_26", "serve"],
+                    help="serve: only the open-loop serving run (its own JSON line)")
+    ap.add_argument("--rate", type=float, default=20.0, help="serving: arrivals per second")
+    ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
+    ap.add_argument("--large", default="h2o_minimal", help="serving: the 5%% large system")
+    ap.add_argument("--max-running", type=int, default=8, help="serving: concurrent jobs")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--fp32-eps", type=float, default=None,
                     help="FP32-tier threshold of the analytic stage (ss_set_eri_tiers); default: the library's")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serve":
+        line = {"metric": "unique ERIs/s under open-loop Poisson arrivals; p50/p99 job latency",
+                "workload": "serve", "serving": serving_run(args.rate, args.duration, args.large, args.max_running)}
+        print(json.dumps(line))
+        return
 
     import torch
     import torch.distributed as dist
@@ -367,6 +398,11 @@ def main():
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
         }
+        if world == 1 and not args.no_serving:
+            try:
+                line["serving"] = serving_run(args.rate, min(args.duration, 10.0), args.large, args.max_running)
+            except Exception as ex:  # reported, not fatal for the throughput line
+                line["serving"] = {"error": str(ex)}
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_baseline(b, q)
             line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -129,14 +129,33 @@ int ss_write_one_e_matrix(const char* path, int n, const double* m);
 
 /* Asynchronous job API (the reference runs one job per process and has none; these queue the
  * job of ss_two_e_job for a serving caller).  ss_job_submit copies the context's basis and
- * quartets and returns at once; the job runs on a worker thread with a private context on the
- * same device, so several jobs overlap on the GPU and later calls on ctx do not affect them.
- * ss_job_poll sets *done = 1 once the job finished; ss_job_result waits for it, copies its eri
- * and sigma (nint each, may be NULL) and forgets the job, returning the job's status code.
- * ss_destroy waits for unfinished jobs and drops their results. */
+ * quartets and returns at once; the job runs on a worker thread with a private worker context
+ * on the same device, so several jobs overlap on the GPU and later calls on ctx do not affect
+ * them.  Worker contexts are kept by ctx and reused by later jobs (their device buffers only
+ * grow).  A job with sigma_target > 0 stops at the first block boundary (after two blocks)
+ * where its largest error bar is at or below the target.  ss_job_poll sets *done = 1 once the
+ * job finished; ss_job_result waits for it, copies its eri and sigma (nint each, may be NULL)
+ * and forgets the job, returning the job's status code.  ss_destroy waits for unfinished jobs,
+ * drops their results and releases the worker contexts. */
 int ss_job_submit(ss_ctx* ctx, double a_zv, uint64_t seed, int64_t samples_per_block, int nblocks,
                   int estimator, int precision, double sigma_target, int64_t* job_id);
+/* The same for a job whose inputs are passed directly (ss_basis_set's and ss_quartets_set's
+ * arrays and meanings): a serving caller submits each request's system without touching the
+ * context's own basis.  The arrays are copied before the call returns; errors in them are
+ * reported by the job (ss_job_result). */
+int ss_job_submit_inputs(ss_ctx* ctx, int nbasis, const double* center, const int* npower,
+                         const int* n_sto, const int* i_type, const int* n_gauss,
+                         const double* c_gauss, int ld, const double* g_gauss,
+                         const double* g_slater, int64_t nint, const int32_t* is,
+                         const int32_t* js, const int32_t* ks, const int32_t* ls, double a_zv,
+                         uint64_t seed, int64_t samples_per_block, int nblocks, int estimator,
+                         int precision, double sigma_target, int64_t* job_id);
 int ss_job_poll(ss_ctx* ctx, int64_t job_id, int* done);
+/* Of a finished job (before ss_job_result): seconds it waited for admission, seconds it ran,
+ * MC blocks it used and its largest error bar (any pointer may be NULL); SS_ERR_STATE while
+ * it runs. */
+int ss_job_info(ss_ctx* ctx, int64_t job_id, double* wait_s, double* run_s, int* blocks,
+                double* max_sigma);
 int ss_job_result(ss_ctx* ctx, int64_t job_id, double* eri, double* sigma);
 
 /* Admission of the asynchronous jobs of this context: a job starts in submission order once

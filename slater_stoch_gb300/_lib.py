@@ -43,7 +43,11 @@ SIGNATURES = {
                                C.c_double, C.c_void_p, C.c_void_p]),
     "ss_job_submit": (C.c_int, [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_int, C.c_int, C.c_int,
                                 C.c_double, C.c_void_p]),
+    "ss_job_submit_inputs": (C.c_int, [C.c_void_p, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, C.c_int, f64p,
+                                       f64p, C.c_int64, i32p, i32p, i32p, i32p, C.c_double, C.c_uint64,
+                                       C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     "ss_job_poll": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "ss_job_info": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ss_job_result": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "ss_write_one_e_matrix": (C.c_int, [C.c_char_p, C.c_int, f64p]),
     "ss_job_limits": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),

@@ -39,6 +39,7 @@ class Context:
         self._h = C.c_void_p(h)
         self.n = 0
         self.nint = 0
+        self._job_nint = {}
 
     # -- lifetime ------------------------------------------------------------------
     def close(self):
@@ -184,6 +185,25 @@ class Context:
         _lib.check(self._L.ss_job_submit(self._h, float(a_zv), int(seed), int(npts), int(nblocks),
                                          ESTIMATORS[estimator], PRECISIONS[precision],
                                          float(sigma_target), _ptr(jid)))
+        self._job_nint[int(jid[0])] = self.nint
+        return int(jid[0])
+
+    def job_submit_inputs(self, b: Basis, quartets, a_zv: float, seed: int, npts: int, nblocks: int,
+                          estimator: str = "shared", precision: str = "split_bf16",
+                          sigma_target: float = 0.0) -> int:
+        """Queue a job on its own system (basis b, quartet lists) without changing this
+        context's basis (ss_job_submit_inputs); returns its id."""
+        a = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
+             np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
+             np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
+             np.ascontiguousarray(b.g_gauss, np.float64).reshape(-1), np.ascontiguousarray(b.g_slater, np.float64)]
+        q = [np.ascontiguousarray(x, np.int32) for x in quartets]
+        jid = np.zeros(1, np.int64)
+        _lib.check(self._L.ss_job_submit_inputs(self._h, int(b.n), a[0], a[1], a[2], a[3], a[4], a[5], int(b.ld),
+                                                a[6], a[7], len(q[0]), *q, float(a_zv), int(seed), int(npts),
+                                                int(nblocks), ESTIMATORS[estimator], PRECISIONS[precision],
+                                                float(sigma_target), _ptr(jid)))
+        self._job_nint[int(jid[0])] = len(q[0])
         return int(jid[0])
 
     def job_poll(self, job_id: int) -> bool:
@@ -191,10 +211,18 @@ class Context:
         _lib.check(self._L.ss_job_poll(self._h, int(job_id), _ptr(done)))
         return bool(done[0])
 
+    def job_info(self, job_id: int) -> dict:
+        """Of a finished job: admission wait and run time (s), MC blocks used, largest sigma."""
+        w, r, m = (np.zeros(1) for _ in range(3))
+        bl = np.zeros(1, np.int32)
+        _lib.check(self._L.ss_job_info(self._h, int(job_id), _ptr(w), _ptr(r), _ptr(bl), _ptr(m)))
+        return {"wait_s": float(w[0]), "run_s": float(r[0]), "blocks": int(bl[0]), "max_sigma": float(m[0])}
+
     def job_result(self, job_id: int):
         """Wait for the job; (eri, sigma).  Raises with the job's own error if it failed."""
-        eri = np.zeros(self.nint)
-        sig = np.zeros(self.nint)
+        nint = self._job_nint.pop(int(job_id), self.nint)
+        eri = np.zeros(nint)
+        sig = np.zeros(nint)
         _lib.check(self._L.ss_job_result(self._h, int(job_id), _ptr(eri), _ptr(sig)))
         return eri, sig
 

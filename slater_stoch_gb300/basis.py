@@ -221,7 +221,38 @@ def build_basis(mol: Molecule, basis: Dict[int, List[Tuple[str, float]]],
 def build_mapping(n: int) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
     """Unique quartets (ik|jl), 1-based, in the reference's order
     (src/build_mapping_ijkl.F90:24-43): l outermost, then k, j >= l, i >= k,
-    keeping i >= j and dropping i == j with l > k."""
+    keeping i >= j and dropping i == j with l > k.
+
+    Built one (l, k) block at a time with numpy: inside a block j runs over l..n and, for each
+    j, i over max(k, j)..n, skipping i == j when l > k (that i is the first of the run)."""
+    npair = n * (n + 1) // 2
+    total = npair * (npair + 1) // 2
+    out = np.empty((4, total), dtype=np.int32)
+    o = 0
+    for l in range(1, n + 1):
+        js = np.arange(l, n + 1, dtype=np.int64)
+        for k in range(1, n + 1):
+            start = np.maximum(k, js) + ((l > k) & (js >= k))
+            cnt = np.maximum(n - start + 1, 0)
+            m = int(cnt.sum())
+            if m == 0:
+                continue
+            jj = np.repeat(js, cnt)
+            first = np.repeat(start - np.cumsum(cnt) + cnt, cnt)  # start of each run, shifted
+            ii = first + np.arange(m)
+            out[0, o:o + m] = ii
+            out[1, o:o + m] = jj
+            out[2, o:o + m] = k
+            out[3, o:o + m] = l
+            o += m
+    if o != total:
+        raise RuntimeError("pb in build_mapping_ijkl")
+    return (np.ascontiguousarray(out[0]), np.ascontiguousarray(out[1]),
+            np.ascontiguousarray(out[2]), np.ascontiguousarray(out[3]))
+
+
+def build_mapping_loops(n: int):
+    """build_mapping written as the reference's four nested loops (kept as its check)."""
     out = []
     for l in range(1, n + 1):
         for k in range(1, n + 1):
@@ -231,12 +262,8 @@ def build_mapping(n: int) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarra
                         continue
                     if i >= j:
                         out.append((i, j, k, l))
-    npair = n * (n + 1) // 2
-    if len(out) != npair * (npair + 1) // 2:
-        raise RuntimeError("pb in build_mapping_ijkl")
     a = np.array(out, dtype=np.int32).reshape(-1, 4)
-    return (np.ascontiguousarray(a[:, 0]), np.ascontiguousarray(a[:, 1]),
-            np.ascontiguousarray(a[:, 2]), np.ascontiguousarray(a[:, 3]))
+    return tuple(np.ascontiguousarray(a[:, c]) for c in range(4))
 
 
 def count_multi_center(b: "Basis", quartets) -> Dict[int, int]:

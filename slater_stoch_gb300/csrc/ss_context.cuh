@@ -41,7 +41,8 @@ struct Mixture {
 }  // namespace ss
 
 namespace ss {
-struct JobState;  // jobs.cu
+struct JobState;    // jobs.cu
+struct WorkerPool;  // jobs.cu: idle worker contexts reused by the jobs
 }
 
 struct ss_ctx {
@@ -98,6 +99,7 @@ struct ss_ctx {
   // asynchronous jobs (jobs.cu) and their admission (admission.h)
   std::map<int64_t, std::shared_ptr<ss::JobState>> jobs;
   std::shared_ptr<ss::JobAdmission> admission;
+  std::shared_ptr<ss::WorkerPool> job_pool;
   int64_t next_job = 1;
   ss::DevBuf d_mean, d_sigma;
 

@@ -190,3 +190,12 @@ def test_library_one_e_writer_matches_fortran_format(tmp_path):
     for name, M in zip(("overlap_ao_ex", "nuclear_ao_ex", "kinetic_ao_ex"), mats):
         output.write_one_e_matrix(tmp_path / (name + ".py"), M)
         assert (tmp_path / name).read_bytes() == (tmp_path / (name + ".py")).read_bytes()
+
+
+def test_build_mapping_matches_reference_loops():
+    """The vectorised quartet map equals the reference's four nested loops
+    (src/build_mapping_ijkl.F90:24-43) element by element, order included."""
+    for n in (1, 2, 3, 4, 7, 13):
+        a = basis.build_mapping(n)
+        b = basis.build_mapping_loops(n)
+        assert all(np.array_equal(x, y) for x, y in zip(a, b)), n
