@@ -188,6 +188,46 @@ def serving_run(rate: float, duration: float, large: str, max_running: int, seed
     return out
 
 
+def random_molecule_run(natoms: int, mol_seed: int, seed: int, rank: int, q: int) -> dict:
+    """The large single-system workload: the seeded random molecule (12 atoms: 111 STOs,
+    1.93e7 unique ERIs), one job to max sigma <= 1e-6 Ha (shared-walker split-BF16 estimator,
+    blocks of 2^20 walker pairs, at most 256 blocks = 2^28), timed with CUDA events on the
+    library stream, then the randomized-SVD cleanup (rank `rank`, q power iterations) of the
+    packed pair metric."""
+    import torch
+    from slater_stoch_gb300 import api, basis, configs
+    b = configs.random_molecule(mol_seed, natoms=natoms)
+    qq = basis.build_mapping(b.n)
+    nint = len(qq[0])
+    npts, nmax = 1 << 20, 256
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*qq)
+        st = torch.cuda.ExternalStream(ctx.stream_ptr)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        ctx.gauss_eri(copy=False)
+        e1.record(st)
+        ctx.zvmc(A_ZV, seed, npts, nmax, "shared", "split_bf16", SIGMA_TARGET, copy=False)
+        e2.record(st)
+        e2.synchronize()
+        t_an, t_mc = e0.elapsed_time(e1) * 1e-3, e1.elapsed_time(e2) * 1e-3
+        out = {"natoms": natoms, "mol_seed": mol_seed, "nbasis": b.n, "unique_eris": nint,
+               "analytic_s": t_an, "mc_s": t_mc, "eris_per_s": nint / (t_an + t_mc),
+               "max_sigma_Ha": ctx.max_sigma, "blocks": ctx.blocks_done, "walkers": ctx.blocks_done * npts,
+               "sigma_target_Ha": SIGMA_TARGET}
+        eri = ctx.combine()
+        out["nonfinite_eris"] = int((~np.isfinite(eri)).sum())
+        try:
+            t = time.perf_counter()
+            _, nrem = ctx.psd_clean(eri, layout="packed_pair", rank=rank, oversample=0, q=q, seed=seed)
+            out.update({"svd_clean_s": time.perf_counter() - t, "svd_clean_removed": nrem,
+                        "svd_clean": f"packed pair metric N={b.n * (b.n + 1) // 2}, rank {rank}, q {q}, FP64"})
+        except Exception as ex:
+            out["svd_clean_error"] = str(ex)
+    return out
+
+
 def fp64_peak_tflops(torch):
     n = 4096
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
@@ -214,8 +254,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="h2o_26", choices=["h2o_26", "serve"],
-                    help="serve: only the open-loop serving run (its own JSON line)")
+    ap.add_argument("--workload", default="h2o_26", choices=["h2o_26", "serve", "random"],
+                    help="serve: only the open-loop serving run; random: only the large random-molecule "
+                         "job (each its own JSON line)")
+    ap.add_argument("--natoms", type=int, default=12, help="random: atoms of the random molecule")
+    ap.add_argument("--mol-seed", type=int, default=1, help="random: seed of the random molecule")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: arrivals per second")
     ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
     ap.add_argument("--large", default="h2o_minimal", help="serving: the 5%% large system")
@@ -226,6 +269,11 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "random":
+        line = {"metric": "unique ERIs/s at sigma<=1e-6 Ha, one large system (seeded random molecule)",
+                "workload": "random", "random": random_molecule_run(args.natoms, args.mol_seed, 1, 512, 4)}
+        print(json.dumps(line))
+        return
     if args.workload == "serve":
         line = {"metric": "unique ERIs/s under open-loop Poisson arrivals; p50/p99 job latency",
                 "workload": "serve", "serving": serving_run(args.rate, args.duration, args.large, args.max_running)}

@@ -32,6 +32,8 @@ extern "C" {
 
 #define SS_EST_FAITHFUL 0      /* per-pair ZV map, src/two_e_slater.F90:401-454 */
 #define SS_EST_SHARED 1        /* one walker set for all pairs (tensor-core contraction) */
+#define SS_JOB_MC_ONLY 256     /* or'ed into a job's estimator: the job returns the MC correction
+                                  (mean) and its error bar instead of the merged ERIs */
 
 #define SS_PREC_FP64 0         /* FP64 arithmetic (src/two_e_slater.F90:443,447 variant) */
 #define SS_PREC_REF32 1        /* the reference's FP32 casts of weight and 1/r12 (:442,:446) */
@@ -58,6 +60,15 @@ int64_t ss_launch_count(const ss_ctx* ctx);
 int ss_basis_set(ss_ctx* ctx, int nbasis, const double* center, const int* npower,
                  const int* n_sto, const int* i_type, const int* n_gauss, const double* c_gauss,
                  int ld, const double* g_gauss, const double* g_slater);
+
+/* No counterpart in the reference (it runs one system per process).  Declares that the basis set
+ * by ss_basis_set holds nsys independent systems, system s being functions first[s] ..
+ * first[s+1]-1 (1-based; first[0] = 1, first[nsys] = nbasis + 1): primitive pairs of functions
+ * of two systems are never formed, so a quartet list that concatenates the systems' own quartets
+ * is evaluated by ss_gauss_eri with one launch per kernel class for all of them.  The ZV-MC
+ * entry points need a single system (SS_ERR_STATE otherwise): run each system's MC as its own
+ * job (SS_JOB_MC_ONLY).  ss_basis_set resets the context to one system. */
+int ss_basis_systems(ss_ctx* ctx, int nsys, const int* first);
 
 /* Replaces is/js/ks/ls of common_data built by build_mapping_ijkl (src/build_mapping_ijkl.F90). */
 int ss_quartets_set(ss_ctx* ctx, int64_t nint, const int32_t* is, const int32_t* js,

@@ -50,6 +50,8 @@ def lib():
         L.orc_gauss_eri.restype = C.c_int64
         L.orc_gauss_eri.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p, i32p, i32p, f64p,
                                     f64p, C.c_int]
+        L.orc_gauss_list.restype = None
+        L.orc_gauss_list.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p, i32p, i32p, f64p, C.c_int]
         L.orc_count_primitive_quartets.restype = C.c_double
         L.orc_count_primitive_quartets.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p,
                                                    i32p, i32p]
@@ -139,6 +141,14 @@ def gauss_eri(ob: OracleBasis, quartets, pre=None, nthreads=0):
     out = np.zeros(len(is_))
     nz = lib().orc_gauss_eri(C.byref(ob.s), len(is_), is_, js, ks, ls, pre, out, _threads(nthreads))
     return out, int(nz)
+
+
+def gauss_list(ob: OracleBasis, quartets, nthreads=0):
+    """gauss_ijkl of each listed (1-based) quartet, no screening or diagonal shortcut."""
+    q = [np.ascontiguousarray(a, np.int32) for a in quartets]
+    out = np.zeros(len(q[0]))
+    lib().orc_gauss_list(C.byref(ob.s), len(q[0]), *q, out, _threads(nthreads))
+    return out
 
 
 def count_primitive_quartets(ob: OracleBasis, quartets):

@@ -703,6 +703,19 @@ int64_t orc_gauss_eri(const orc_basis *b, int64_t nint, const int32_t *is, const
   return nzero;
 }
 
+/* gauss_ijkl of every listed quartet, no Schwarz screening and no diagonal shortcut (the
+ * entries of the Schwarz diagonal a subset of quartets needs, src/two_e_slater.F90:230-236) */
+void orc_gauss_list(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                    const int32_t *ks, const int32_t *ls, double *out, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t q = 0; q < nint; q++) out[q] = orc_gauss_ijkl(b, is[q] - 1, ks[q] - 1, js[q] - 1, ls[q] - 1);
+}
+
 /* ------------------------------------------------------------------ */
 /* walker transform (src/dierfc.F90:3-68)                              */
 /* ------------------------------------------------------------------ */

@@ -69,6 +69,8 @@ void orc_precond(const orc_basis *b, double *precond, int nthreads);
 int64_t orc_gauss_eri(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
                       const int32_t *ks, const int32_t *ls, const double *precond,
                       double *out, int nthreads);
+void orc_gauss_list(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                    const int32_t *ks, const int32_t *ls, double *out, int nthreads);
 
 /* primitive-quartet count of the sweep (sum over quartets of prod n_gauss*nc) */
 double orc_count_primitive_quartets(const orc_basis *b, int64_t nint, const int32_t *is,

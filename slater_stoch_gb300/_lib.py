@@ -29,6 +29,7 @@ SIGNATURES = {
     "ss_basis_set": (C.c_int, [C.c_void_p, C.c_int, f64p, i32p, i32p, i32p, i32p, f64p, C.c_int,
                                f64p, f64p]),
     "ss_quartets_set": (C.c_int, [C.c_void_p, C.c_int64, i32p, i32p, i32p, i32p]),
+    "ss_basis_systems": (C.c_int, [C.c_void_p, C.c_int, i32p]),
     "ss_precond": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ss_gauss_eri": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "ss_zvmc": (C.c_int, [C.c_void_p, C.c_double, C.c_uint64, C.c_int64, C.c_int, C.c_int, C.c_int,

@@ -190,9 +190,10 @@ class Context:
 
     def job_submit_inputs(self, b: Basis, quartets, a_zv: float, seed: int, npts: int, nblocks: int,
                           estimator: str = "shared", precision: str = "split_bf16",
-                          sigma_target: float = 0.0) -> int:
+                          sigma_target: float = 0.0, mc_only: bool = False) -> int:
         """Queue a job on its own system (basis b, quartet lists) without changing this
-        context's basis (ss_job_submit_inputs); returns its id."""
+        context's basis (ss_job_submit_inputs); returns its id.  mc_only: the job returns the
+        MC correction and its error bar instead of the merged ERIs (SS_JOB_MC_ONLY)."""
         a = [np.ascontiguousarray(b.center, np.float64).reshape(-1), np.ascontiguousarray(b.npower, np.int32).reshape(-1),
              np.ascontiguousarray(b.n_sto, np.int32), np.ascontiguousarray(b.i_type, np.int32),
              np.ascontiguousarray(b.n_gauss, np.int32), np.ascontiguousarray(b.c_gauss, np.float64).reshape(-1),
@@ -201,8 +202,8 @@ class Context:
         jid = np.zeros(1, np.int64)
         _lib.check(self._L.ss_job_submit_inputs(self._h, int(b.n), a[0], a[1], a[2], a[3], a[4], a[5], int(b.ld),
                                                 a[6], a[7], len(q[0]), *q, float(a_zv), int(seed), int(npts),
-                                                int(nblocks), ESTIMATORS[estimator], PRECISIONS[precision],
-                                                float(sigma_target), _ptr(jid)))
+                                                int(nblocks), ESTIMATORS[estimator] | (256 if mc_only else 0),
+                                                PRECISIONS[precision], float(sigma_target), _ptr(jid)))
         self._job_nint[int(jid[0])] = len(q[0])
         return int(jid[0])
 

@@ -63,8 +63,9 @@ __global__ void prim_pair_count(BasisDev B, int npairs, int* __restrict__ cnt) {
   const double* A = B.center + 3 * i;
   const double* Bc = B.center + 3 * k;
   const bool fold = fold_pair(B, i, k);
+  const bool other_system = B.sys && B.sys[i] != B.sys[k];
   int local = 0;
-  for (int t = threadIdx.x; t < ngi * ngk; t += blockDim.x) {
+  for (int t = threadIdx.x; t < (other_system ? 0 : ngi * ngk); t += blockDim.x) {
     int m1 = t / ngk, m2 = t % ngk;
     if (fold && m2 < m1) continue;  // folded into (m2, m1), see prim_pair_fill
     double a = B.g_gauss[m1 + (int64_t)B.ld * i], b = B.g_gauss[m2 + (int64_t)B.ld * k];
@@ -98,6 +99,7 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
   // For a folded pair (fold_pair) only m1 <= m2 is kept, with the coefficient doubled for
   // m1 < m2 (exact), which halves the primitive pairs of those function pairs.
   if (threadIdx.x != 0) return;
+  if (B.sys && B.sys[i] != B.sys[k]) return;  // functions of two systems: no pairs
   const bool fold = fold_pair(B, i, k);
   int64_t o = off[pidx];
   for (int m1 = 0; m1 < ngi; m1++)
@@ -170,7 +172,7 @@ void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem) {
   // SM (8 warps) and leave unified L1 to the local arrays of the classes with r^2-type fits.  On
   // the 26-function H2O basis 168 KB (one CTA per SM) -> 60 KB tiles took the analytic stage from
   // 2.71 to 2.53 s.
-  const size_t budget = 60u * 1024u;
+  const size_t budget = (size_t)ERI_SMEM_MAX;
   int kt = (int)(budget / per);
   kt = kt < max_cnt ? kt : max_cnt;
   kt = kt < 1 ? 1 : kt;

@@ -7,7 +7,7 @@ cudaError_t launch_eri_L2c0(dim3 grid, int ktile, size_t smem, cudaStream_t st, 
                                int split, const int32_t* is, const int32_t* js, const int32_t* ks,
                                const int32_t* ls, const double* pre, double eps, double eps32, double* partial,
                                double* self_out, const PrimPairF* ppf) {
-  cudaError_t e = cudaFuncSetAttribute(eri_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(eri_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ERI_SMEM_MAX);
   if (e != cudaSuccess) return e;
   eri_kernel<2, 0><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, pre, eps, eps32, partial,
                                                self_out, ppf);

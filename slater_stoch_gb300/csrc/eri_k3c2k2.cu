@@ -9,7 +9,7 @@ cudaError_t launch_eri_L3c2k2(dim3 grid, int ktile, size_t smem, cudaStream_t st
                                   const int32_t* ls, const double* pre, double eps, double eps32, double* partial,
                                   double* self_out, const PrimPairF* ppf) {
   cudaError_t e =
-      cudaFuncSetAttribute(eri_kernel<3, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(eri_kernel<3, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ERI_SMEM_MAX);
   if (e != cudaSuccess) return e;
   eri_kernel<3, 2, 2><<<grid, 128, smem, st>>>(B, pp, off, cnt, work, split, ktile, is, js, ks, ls, pre, eps, eps32,
                                                   partial, self_out, ppf);

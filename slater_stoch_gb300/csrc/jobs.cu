@@ -117,7 +117,10 @@ static int submit(ss_ctx* c, std::shared_ptr<JobInputs> in, double a_zv, uint64_
       if (!rc) rc = ss_quartets_set(w, in->nint, in->is.data(), in->js.data(), in->ks.data(), in->ls.data());
       if (!rc) rc = ss_set_exact_monocenter(w, in->exact_mono ? 1 : 0);
       if (!rc) rc = ss_set_eri_tiers(w, in->eps_screen, in->eps32);
-      if (!rc)
+      if (!rc && (estimator & SS_JOB_MC_ONLY))  // the MC correction and its error bar only
+        rc = ss_zvmc(w, a_zv, seed, samples_per_block, nblocks, estimator & ~SS_JOB_MC_ONLY, precision,
+                     sigma_target, st->eri.data(), st->sigma.data());
+      else if (!rc)
         rc = ss_two_e_job(w, a_zv, seed, samples_per_block, nblocks, estimator, precision, sigma_target,
                           st->eri.data(), st->sigma.data());
       if (rc) {
@@ -170,6 +173,10 @@ int ss_job_submit(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_blo
   }
   if (!c->n || !c->nint) {
     ss_set_error_msg("ss_job_submit needs ss_basis_set and ss_quartets_set first");
+    return SS_ERR_STATE;
+  }
+  if (!c->h_sys.empty() && c->h_sys.back() > 0) {
+    ss_set_error_msg("ss_job_submit: the basis holds several systems; submit each with ss_job_submit_inputs");
     return SS_ERR_STATE;
   }
   auto in = std::make_shared<JobInputs>();

@@ -183,64 +183,107 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// r = sqrt(f^2 + g^2) and 1/r.  FP64 square roots and divisions take tens of FP64-pipe
+// instructions, which GB300 issues at two per clock per SM; this takes the FP32 reciprocal
+// square root of x = f^2 + g^2 as the seed and two Newton steps y <- y (3/2 - x y^2 / 2), each
+// doubling the correct bits (24 -> 48 -> FP64 rounding), for a few FP64 fused multiply-adds.
+// Outside the FP32 range of x it falls back to hypot and a division.
+__device__ __forceinline__ void hypot_inv(double f, double g, double& r, double& rinv) {
+  const double x = fma(f, f, g * g);
+  if (!(x > 1e-36 && x < 1e36)) {
+    r = hypot(f, g);
+    rinv = r > 0.0 ? 1.0 / r : 0.0;
+    return;
+  }
+  double y = (double)rsqrtf((float)x);
+  const double hx = 0.5 * x;
+  y = y * fma(-hx * y, y, 1.5);
+  y = y * fma(-hx * y, y, 1.5);
+  rinv = y;
+  r = x * y;
+}
+
 // Panel j0 .. j0+b-1 of Z (rows j0 .. N-1): Householder vectors in place below the diagonal
 // (unit leading entry implied), and explicitly into Vb(:, j0 .. j0+b-1) (zeros above, 1 on the
 // diagonal); T (QR_NB x QR_NB col-major, upper triangular) with H_j0 ... H_{j0+b-1} =
-// I - V T V^T (the forward column-wise recurrence of LAPACK's dlarft).  1024 threads.
+// I - V T V^T (the forward column-wise recurrence of LAPACK's dlarft).  1024 threads.  With
+// SMEM the panel's mr = N - j0 rows are staged in shared memory (mr x b doubles), so the
+// column-by-column steps read no global memory; otherwise it is factorised in place.
+template <bool SMEM>
 __global__ void __launch_bounds__(1024) qr_panel_kernel(int N, int j0, int b, double* __restrict__ Z, int ld,
                                                         double* __restrict__ Vb, double* __restrict__ T) {
+  extern __shared__ double s_panel[];
   __shared__ double sh[32];
   __shared__ double s_tau[QR_NB];
   __shared__ double s_G[QR_NB][QR_NB + 1];
   __shared__ double s_T[QR_NB][QR_NB + 1];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int mr = N - j0;
+  double* X = SMEM ? s_panel : Z + j0 + (size_t)j0 * ld;  // X(i, jj), i < mr
+  const int ldx = SMEM ? mr : ld;
+  if (SMEM) {
+    for (int e = threadIdx.x; e < mr * b; e += blockDim.x) {
+      const int i = e % mr, jj = e / mr;
+      X[i + (size_t)jj * ldx] = Z[j0 + i + (size_t)(j0 + jj) * ld];
+    }
+    __syncthreads();
+  }
   for (int jj = 0; jj < b; jj++) {
-    const int c = j0 + jj;
-    double* x = Z + (size_t)c * ld;
+    double* x = X + (size_t)jj * ldx;
     double ss = 0.0;
-    for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) ss += x[i] * x[i];
+    for (int i = jj + 1 + threadIdx.x; i < mr; i += blockDim.x) ss += x[i] * x[i];
     const double sigma = block_sum(ss, sh);
-    const double x0 = x[c];
+    const double x0 = x[jj];
     double tau = 0.0;
     if (sigma != 0.0) {
       const double mu = sqrt(x0 * x0 + sigma);
       const double alpha = x0 <= 0.0 ? mu : -mu;  // R_cc, sign chosen against cancellation
       const double v0 = x0 - alpha;
       const double inv = 1.0 / v0;
-      for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) x[i] *= inv;
+      for (int i = jj + 1 + threadIdx.x; i < mr; i += blockDim.x) x[i] *= inv;
       tau = -v0 / alpha;
       __syncthreads();
-      if (threadIdx.x == 0) x[c] = alpha;
+      if (threadIdx.x == 0) x[jj] = alpha;
     }
     if (threadIdx.x == 0) s_tau[jj] = tau;
     __syncthreads();
-    // H_c applied to the panel's remaining columns, one warp per column
+    // H applied to the panel's remaining columns, one warp per column
     if (tau != 0.0)
-      for (int cc = c + 1 + warp; cc < j0 + b; cc += blockDim.x >> 5) {
-        double* z = Z + (size_t)cc * ld;
-        double s = lane == 0 ? z[c] : 0.0;
-        for (int i = c + 1 + lane; i < N; i += 32) s += x[i] * z[i];
+      for (int cc = jj + 1 + warp; cc < b; cc += nw) {
+        double* z = X + (size_t)cc * ldx;
+        double s = lane == 0 ? z[jj] : 0.0;
+        for (int i = jj + 1 + lane; i < mr; i += 32) s += x[i] * z[i];
         const double w = tau * warp_sum(s);
-        if (lane == 0) z[c] -= w;
-        for (int i = c + 1 + lane; i < N; i += 32) z[i] -= w * x[i];
+        if (lane == 0) z[jj] -= w;
+        for (int i = jj + 1 + lane; i < mr; i += 32) z[i] -= w * x[i];
       }
     __syncthreads();
   }
-  // explicit V of the panel
-  for (int jj = 0; jj < b; jj++) {
-    const int c = j0 + jj;
-    for (int i = threadIdx.x; i < N; i += blockDim.x)
-      Vb[i + (size_t)c * N] = i < c ? 0.0 : (i == c ? 1.0 : Z[i + (size_t)c * ld]);
+  // factored panel back to Z; explicit V of the panel
+  for (int e = threadIdx.x; e < N * b; e += blockDim.x) {
+    const int i = e % N, jj = e / N, c = j0 + jj;
+    const double v = i >= j0 ? X[(i - j0) + (size_t)jj * ldx] : 0.0;
+    if (SMEM && i >= j0) Z[i + (size_t)c * ld] = v;
+    Vb[i + (size_t)c * N] = i < c ? 0.0 : (i == c ? 1.0 : v);
   }
   __syncthreads();
-  // G = V^T V of the panel (rows j0 .. N-1), one warp per entry
-  for (int e = warp; e < b * b; e += blockDim.x >> 5) {
+  // G = V^T V of the panel, one warp per entry (from the staged rows when SMEM)
+  for (int e = warp; e < b * b; e += nw) {
     const int r = e % b, cc = e / b;
     if (r > cc) continue;
-    const double* vr = Vb + (size_t)(j0 + r) * N;
-    const double* vc = Vb + (size_t)(j0 + cc) * N;
     double s = 0.0;
-    for (int i = j0 + lane; i < N; i += 32) s += vr[i] * vc[i];
+    if (SMEM) {
+      // V(i, r) = 1 at i = r, X(i, r) below, 0 above
+      for (int i = cc + lane; i < mr; i += 32) {
+        const double vr = i == r ? 1.0 : (i > r ? X[i + (size_t)r * ldx] : 0.0);
+        const double vc = i == cc ? 1.0 : X[i + (size_t)cc * ldx];
+        s += vr * vc;
+      }
+    } else {
+      const double* vr = Vb + (size_t)(j0 + r) * N;
+      const double* vc = Vb + (size_t)(j0 + cc) * N;
+      for (int i = j0 + lane; i < N; i += 32) s += vr[i] * vc[i];
+    }
     s = warp_sum(s);
     if (lane == 0) {
       s_G[r][cc] = s;
@@ -267,6 +310,8 @@ __global__ void __launch_bounds__(1024) qr_panel_kernel(int N, int j0, int b, do
     T[e] = (r < b && cc < b) ? s_T[r][cc] : 0.0;
   }
 }
+
+constexpr size_t QR_PANEL_SMEM_MAX = 200 * 1024;  // staged panel (doubles of mr x b)
 
 __global__ void set_identity_cols(int N, int r, double* Q, int ld) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -301,7 +346,14 @@ int ortho_qr(cudaStream_t st, int N, int r, double* Z, int ld, double* work, int
   for (int p = 0; p < P; p++) {
     const int j0 = p * QR_NB, b = std::min(QR_NB, r - j0), nc = r - j0 - b, mr = N - j0;
     double* Tp = T + (size_t)QR_NB * QR_NB * p;
-    qr_panel_kernel<<<1, 1024, 0, st>>>(N, j0, b, Z, ld, Vb, Tp);
+    const size_t psmem = sizeof(double) * (size_t)mr * b;
+    if (psmem <= QR_PANEL_SMEM_MAX) {
+      SS_CUDA_TRY(cudaFuncSetAttribute(qr_panel_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)QR_PANEL_SMEM_MAX));
+      qr_panel_kernel<true><<<1, 1024, psmem, st>>>(N, j0, b, Z, ld, Vb, Tp);
+    } else {
+      qr_panel_kernel<false><<<1, 1024, 0, st>>>(N, j0, b, Z, ld, Vb, Tp);
+    }
     SS_CUDA_TRY(cudaGetLastError());
     if (launches) (*launches)++;
     if (nc > 0) {  // trailing columns: C <- (I - V T^T V^T) C
@@ -365,8 +417,9 @@ __global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double*
         if (tid == 0) e[i] = A(i, l);
       } else {
         double hh = 0.0;
+        const double sinv = 1.0 / scale;
         for (int k = tid; k <= l; k += nt) {
-          const double v = A(i, k) / scale;
+          const double v = A(i, k) * sinv;
           A(i, k) = v;
           hh += v * v;
         }
@@ -379,6 +432,7 @@ __global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double*
           A(i, l) = f0 - g0;
         }
         h = h - f0 * g0;
+        const double hinv = 1.0 / h;
         __syncthreads();
         // p = A u / h (u = row i, entries 0..l) into e[0..l]: one warp per row j
         for (int j = tid >> 5; j <= l; j += nt >> 5) {
@@ -386,8 +440,8 @@ __global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double*
           for (int k = (tid & 31); k <= l; k += 32) g += (k <= j ? A(j, k) : A(k, j)) * A(i, k);
           g = warp_sum(g);
           if ((tid & 31) == 0) {
-            A(j, i) = A(i, j) / h;
-            e[j] = g / h;
+            A(j, i) = A(i, j) * hinv;
+            e[j] = g * hinv;
           }
         }
         __syncthreads();
@@ -473,7 +527,8 @@ __global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double*
             bool underflow = false;
             for (int i = m - 1; i >= l; i--) {
               double f = s * e[i], bb = c * e[i];
-              r = hypot(f, g);
+              double rinv;
+              hypot_inv(f, g, r, rinv);
               e[i + 1] = r;
               if (r == 0.0) {
                 d[i + 1] -= p;
@@ -481,8 +536,8 @@ __global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double*
                 underflow = true;
                 break;
               }
-              s = f / r;
-              c = g / r;
+              s = f * rinv;
+              c = g * rinv;
               g = d[i + 1] - p;
               r = (d[i] - g) * s + 2.0 * c * bb;
               p = s * r;
@@ -607,14 +662,15 @@ __global__ void jacobi_maxabs(int64_t nn, const double* __restrict__ A, JacobiCt
 __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__ A0, double* __restrict__ A1,
                                                      double* __restrict__ V, double* __restrict__ d,
                                                      JacobiCtl* ctl, int* err) {
-  extern __shared__ double s_cs[];  // c[np], s[np], t[np]
+  extern __shared__ double s_cs[];  // c[np], s[np]
   __shared__ int s_rot;
   const int np = (n + 1) / 2, np2 = 2 * np;
   double* sc = s_cs;
   double* ss = sc + np;
-  double* st_ = ss + np;
   const double eps = 2.2204460492503131e-16;
-  const double tiny = 0.1 * eps * ctl->amax;  // rounding level of the matrix entries
+  const double amax = ctl->amax;
+  const double tiny = 0.1 * eps * amax;  // rounding level of the matrix entries
+  const double inv_amax = amax > 0.0 ? 1.0 / amax : 0.0;
   const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // V = I
@@ -633,20 +689,32 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
       for (int pi = threadIdx.x; pi < np; pi += blockDim.x) {
         int p = rr_player(pi, round, np2), q = rr_player(np2 - 1 - pi, round, np2);
         if (p > q) { const int t = p; p = q; q = t; }
-        double c = 1.0, s = 0.0, t = 0.0;
+        double c = 1.0, s = 0.0;
         if (q < n) {
           const double apq = cur[p + (size_t)q * n], app = cur[p + (size_t)p * n], aqq = cur[q + (size_t)q * n];
-          if (fabs(apq) > fmax(eps * sqrt(fabs(app) * fabs(aqq)), tiny)) {
-            const double tau = (aqq - app) / (2.0 * apq);
-            t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
+          // skip below the rounding level, or below eps of the diagonal pair (compared squared)
+          if (fabs(apq) > tiny && apq * apq > eps * eps * fabs(app) * fabs(aqq)) {
+            // the angle in FP32 on entries scaled by 1/max|A| (t = tan(theta) of the rotation that
+            // zeroes apq; the symmetric Schur form of Golub and Van Loan), then (c, s) made
+            // orthonormal in FP64: c^2 + s^2 = 1 - e, scaled by (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8.
+            // An FP32 angle leaves about 1e-7 of apq for the next sweep; the rotation itself is
+            // orthogonal to FP64 precision.
+            const float dq = (float)((aqq - app) * inv_amax), pq = (float)(apq * inv_amax);
+            const float tau = dq / (2.0f * pq);
+            const float at = fabsf(tau);
+            const float t = at > 1e15f ? 0.5f / tau : copysignf(1.0f, tau) / (at + sqrtf(1.0f + at * at));
+            const float cf = rsqrtf(1.0f + t * t);
+            c = (double)cf;
+            s = (double)(t * cf);
+            const double e = 1.0 - fma(c, c, s * s);
+            const double r = fma(e, fma(0.375, e, 0.5), 1.0);
+            c *= r;
+            s *= r;
             myrot++;
           }
         }
         sc[pi] = c;
         ss[pi] = s;
-        st_[pi] = t;
       }
       if (blockIdx.x == 0 && myrot) atomicAdd(&s_rot, myrot);
       __syncthreads();
@@ -664,25 +732,20 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
         if (r > s2) { const int t = r; r = s2; s2 = t; }
         const double cP = sc[P], sP = ss[P], cR = sc[R], sR = ss[R];
         const bool qv = q < n, sv = s2 < n;
-        if (P == R) {  // diagonal block: the rotation's own exact update
-          const double tP = st_[P];
+        if (P == R) {  // diagonal block J^T A_PP J, its off-diagonal entry symmetrised
           const double app = cur[p + (size_t)p * n];
           if (!qv) {
             nxt[p + (size_t)p * n] = app;
             continue;
           }
           const double apq = cur[p + (size_t)q * n], aqq = cur[q + (size_t)q * n];
-          if (sP == 0.0) {
-            nxt[p + (size_t)p * n] = app;
-            nxt[q + (size_t)q * n] = aqq;
-            nxt[p + (size_t)q * n] = apq;
-            nxt[q + (size_t)p * n] = apq;
-          } else {
-            nxt[p + (size_t)p * n] = app - tP * apq;
-            nxt[q + (size_t)q * n] = aqq + tP * apq;
-            nxt[p + (size_t)q * n] = 0.0;
-            nxt[q + (size_t)p * n] = 0.0;
-          }
+          const double xpp = cP * app - sP * apq, xpq = cP * apq - sP * aqq;
+          const double xqp = sP * app + cP * apq, xqq = sP * apq + cP * aqq;
+          nxt[p + (size_t)p * n] = cP * xpp - sP * xpq;
+          nxt[q + (size_t)q * n] = sP * xqp + cP * xqq;
+          const double bpq = 0.5 * ((sP * xpp + cP * xpq) + (cP * xqp - sP * xqq));
+          nxt[p + (size_t)q * n] = bpq;
+          nxt[q + (size_t)p * n] = bpq;
           continue;
         }
         const double a_pr = cur[p + (size_t)r * n];
@@ -765,7 +828,10 @@ int sym_eig(cudaStream_t st, int n, const double* A, double* V, double* w, doubl
   }
   if (n <= EIG_SMEM_MAX) {
     const size_t smem = sizeof(double) * ((size_t)n * n + 5 * (size_t)n);
-    SS_CUDA_TRY(cudaFuncSetAttribute(sym_eig_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the opt-in is per kernel, not per launch: always the largest size, so that threads launching
+    // different sizes at once never lower it under another's launch
+    const int smem_max = (int)(sizeof(double) * (EIG_SMEM_MAX * EIG_SMEM_MAX + 5 * EIG_SMEM_MAX));
+    SS_CUDA_TRY(cudaFuncSetAttribute(sym_eig_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
     sym_eig_smem_kernel<<<1, 1024, smem, st>>>(n, A, V, w, d_err);
     SS_CUDA_TRY(cudaGetLastError());
     if (launches) (*launches)++;
@@ -782,8 +848,9 @@ int sym_eig(cudaStream_t st, int n, const double* A, double* V, double* w, doubl
   SS_CUDA_TRY(cudaGetLastError());
   // one cooperative grid, all CTAs co-resident
   const int np = (n + 1) / 2;
-  const size_t smem = sizeof(double) * 3 * np;
-  SS_CUDA_TRY(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = sizeof(double) * 2 * np;
+  SS_CUDA_TRY(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(double) * 2 * ((4096 + 1) / 2))));  // the largest n
   int per_sm = 0;
   SS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_kernel, 256, smem));
   const int64_t want = std::max<int64_t>(1, ((int64_t)np * (np + 1) / 2 + 255) / 256);

@@ -244,6 +244,10 @@ int ss_zvmc(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_block, in
     ss_set_error_msg("ss_zvmc: need samples_per_block > 0, nblocks > 0, a_zv > 0");
     return SS_ERR_ARG;
   }
+  if (!c->h_sys.empty() && c->h_sys.back() > 0) {
+    ss_set_error_msg("ss_zvmc: the basis holds several systems (ss_basis_systems); run each system's MC as its own job");
+    return SS_ERR_STATE;
+  }
   int rc;
   if (estimator == SS_EST_FAITHFUL) {
     if (samples_per_block % 40 != 0) {  // src/two_e_slater.F90:148

@@ -227,6 +227,8 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   return launch_rc;
 }
 
+int build_pair_tables(ss_ctx* c);
+
 int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out) {
   DevBuf& b = c->pool[name];
   int rc = dev_alloc(c, b, bytes);
@@ -282,8 +284,11 @@ int ensure_precond(ss_ctx* c) {
   DevBuf di, dk;
   int rc = h2d(c, di, qi.data(), sizeof(int32_t) * np);
   if (!rc) rc = h2d(c, dk, qk.data(), sizeof(int32_t) * np);
-  std::vector<int64_t> sel(np), slot;
-  std::iota(sel.begin(), sel.end(), 0);
+  // a pair without primitive pairs (all screened, or functions of two systems) has (ik|ik) = 0
+  std::vector<int64_t> sel, slot;
+  sel.reserve(np);
+  for (int64_t p = 0; p < np; p++)
+    if (c->h_pp_cnt[p] > 0) sel.push_back(p);
   int64_t npartial = 0;
   // 1. primitive-pair Schwarz factors (items (P,P) of the diagonal quartets) into pad[0],
   // 2. per-pair sort by decreasing factor, 3. the diagonal quartets themselves
@@ -317,7 +322,8 @@ int ensure_precond(ss_ctx* c) {
   c->h_precond.assign((size_t)n * n, 0.0);
   for (int64_t p = 0; p < np; p++) {
     double v = 0.0;
-    for (int t = 0; t < slot_split(slot[p]); t++) v = v + part[slot_offset(slot[p]) + t];
+    if (slot[p] >= 0)
+      for (int t = 0; t < slot_split(slot[p]); t++) v = v + part[slot_offset(slot[p]) + t];
     int i = qi[p] - 1, k = qk[p] - 1;
     c->h_precond[i + (size_t)n * k] = v;
     c->h_precond[k + (size_t)n * i] = v;
@@ -452,7 +458,7 @@ void ss_destroy(ss_ctx* c) {
                     &c->d_gs, &c->d_pp, &c->d_ppf, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
                     &c->d_ls, &c->d_precond, &c->d_gauss, &c->d_mean, &c->d_sigma, &c->d_scratch_a,
                     &c->d_scratch_b, &c->d_scratch_c, &c->d_scratch_d, &c->d_mono_val, &c->d_mono_mask,
-                    &c->d_mono_status};
+                    &c->d_mono_status, &c->d_sys};
   for (DevBuf* b : bufs) dev_free(c, *b);
   for (auto& kv : c->pool) dev_free(c, kv.second);
   for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
@@ -528,9 +534,45 @@ int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower,
   if (rc) return SS_ERR_NOMEM;
   c->basis = BasisDev{nbasis, ld, (const double*)c->d_center.ptr, (const int*)c->d_npower.ptr,
                       (const int*)c->d_nsto.ptr, (const int*)c->d_itype.ptr, (const int*)c->d_ng.ptr,
-                      (const double*)c->d_cg.ptr, (const double*)c->d_gg.ptr, (const double*)c->d_gs.ptr};
-  // primitive-pair tables
+                      (const double*)c->d_cg.ptr, (const double*)c->d_gg.ptr, (const double*)c->d_gs.ptr,
+                      nullptr};
+  c->h_sys.clear();
+  return build_pair_tables(c);
+}
+
+int ss_basis_systems(ss_ctx* c, int nsys, const int* first) {
+  SS_CHECK_CTX(c);
+  if (!c->n) {
+    ss_set_error_msg("ss_basis_systems needs ss_basis_set first");
+    return SS_ERR_STATE;
+  }
+  if (nsys < 1 || !first || first[0] != 1 || first[nsys] != c->n + 1) {
+    ss_set_error_msg("ss_basis_systems: need nsys >= 1 and first[0] = 1, first[nsys] = nbasis + 1");
+    return SS_ERR_ARG;
+  }
+  std::vector<int> sys(c->n);
+  for (int s = 0; s < nsys; s++) {
+    if (first[s + 1] <= first[s]) {
+      ss_set_error_msg("ss_basis_systems: system %d is empty or out of order", s + 1);
+      return SS_ERR_ARG;
+    }
+    for (int f = first[s] - 1; f < first[s + 1] - 1; f++) sys[f] = s;
+  }
+  int rc = h2d(c, c->d_sys, sys.data(), sizeof(int) * c->n);
+  if (rc) return rc;
+  c->h_sys = sys;
+  c->basis.sys = (const int*)c->d_sys.ptr;
+  return build_pair_tables(c);
+}
+
+}  // extern "C"
+
+namespace ss {
+// Primitive-pair tables of every function pair i >= k (pairs across systems have none)
+int build_pair_tables(ss_ctx* c) {
+  const int nbasis = c->n;
   int npairs = nbasis * (nbasis + 1) / 2;
+  int rc;
   rc = dev_alloc(c, c->d_pp_cnt, sizeof(int) * npairs);
   if (rc) return rc;
   SS_CUDA_TRY(eri_init_constants());
@@ -555,6 +597,9 @@ int ss_basis_set(ss_ctx* c, int nbasis, const double* center, const int* npower,
   c->have_resid = c->have_mono = false;
   return SS_OK;
 }
+}  // namespace ss
+
+extern "C" {
 
 int ss_quartets_set(ss_ctx* c, int64_t nint, const int32_t* is, const int32_t* js, const int32_t* ks,
                     const int32_t* ls) {

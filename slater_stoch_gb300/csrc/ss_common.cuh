@@ -28,6 +28,10 @@ constexpr int SS_MAX_NF = 24;        // highest Boys order F_n used by one primi
 // per function pair the skipped part of an ERI is below 8.1e5 * 1e-18 = 8.1e-13 of its Schwarz
 // bound sqrt((ik|ik)(jl|jl)), and in practice far below (the bound is loose, the signs vary).
 constexpr double PRIM_SCREEN_EPS = 1e-18;
+// Dynamic shared memory of one ERI-kernel CTA (ket tiles and their polynomials) never exceeds
+// this; every launch opts in to exactly this much, so concurrent launches from several host
+// threads (jobs) all set the same per-kernel attribute (a per-launch size would race).
+constexpr int ERI_SMEM_MAX = 60 * 1024;
 // Where a quartet's partial sums (one per bra slice) live: slot code = offset << SLOT_SPLIT_BITS |
 // split, the partials being entries offset .. offset + split - 1 (split < 2^SLOT_SPLIT_BITS).
 constexpr int SLOT_SPLIT_BITS = 7;
@@ -74,6 +78,8 @@ struct BasisDev {
   const double* c_gauss;  // [ld*n*2]
   const double* g_gauss;  // [ld*n]
   const double* g_slater; // [n]
+  const int* sys;         // [n] system of each function when several systems share the basis
+                          // (ss_basis_systems; pairs across systems are never formed), or null
 };
 
 __host__ __device__ inline int64_t ss_pair_index(int i, int k) {  // i >= k, 0-based

@@ -62,6 +62,8 @@ struct ss_ctx {
   std::vector<double> h_center, h_gg, h_cg, h_gs;
   std::vector<int> h_npower, h_nsto, h_itype, h_ng;
   ss::DevBuf d_center, d_npower, d_nsto, d_itype, d_ng, d_cg, d_gg, d_gs;
+  std::vector<int> h_sys;  // system of each function (ss_basis_systems), empty for one system
+  ss::DevBuf d_sys;
   ss::BasisDev basis{};
 
   // nuclei for the one-electron nuclear attraction (ss_nuclei_set)

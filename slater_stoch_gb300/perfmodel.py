@@ -31,6 +31,26 @@ def _pair_L(b, f1, f2):
     return int(max(b.npower[f1, ax] + t1 + b.npower[f2, ax] + t2 for ax in range(3)))
 
 
+def kernel_classes(b, quartets):
+    """The analytic kernel instance (L, LK, tc) of every quartet, as the device buckets them:
+    L = the larger pair's per-axis degree bound, tc = the number of r^2-type fits among the four
+    functions, LK = the lighter pair's bound (1 or 2) for L >= 3 quartets whose lighter pair has
+    L <= 2, else L.  Returns an (nq, 3) int array."""
+    is_, js, ks, ls = [np.asarray(a) - 1 for a in quartets]
+    n = b.n
+    PL = np.zeros((n, n), dtype=np.int64)
+    for i in range(n):
+        for k in range(n):
+            PL[i, k] = _pair_L(b, i, k)
+    Lb, Lk = PL[is_, ks], PL[js, ls]
+    L = np.maximum(Lb, Lk)
+    lmin = np.minimum(Lb, Lk)
+    r2 = (np.asarray(b.i_type) == 2).astype(np.int64)
+    tc = r2[is_] + r2[ks] + r2[js] + r2[ls]
+    LK = np.where((L >= 3) & (lmin <= 2), np.maximum(lmin, 1), L)
+    return np.stack([L, LK, tc], axis=1)
+
+
 def primitive_quartets_by_class(b, quartets):
     """{L: primitive quartets} summed over the quartet list (no K_AB screening)."""
     is_, js, ks, ls = [np.asarray(a) - 1 for a in quartets]

@@ -132,3 +132,45 @@ def test_gauss_eri_golden_ng20():
         ctx.set_quartets(*q)
         g, nz = ctx.gauss_eri()
     _check(g, fx["eri_ext"], fx["precond"], q)
+
+
+def test_gauss_eri_random_molecule_subset():
+    """The large single-system workload: the seeded 12-atom random molecule (111 STOs, 20-Gaussian
+    fits, 1.93e7 unique quartets).  The device computes the whole Schwarz diagonal (6,216
+    quartets (ik|ik)) and the ERIs of a subset: >= 8 quartets of every kernel instance
+    (L, LK, tc) and 60 more at random; the oracle computes the same quartets and the diagonal
+    entries they need.  Gate per quartet: 1e-12 |ERI| + 1e-12 sqrt((ik|ik)(jl|jl))."""
+    from slater_stoch_gb300 import perfmodel
+    O = _oracle()
+    b = configs.random_molecule(1)
+    q = basis.build_mapping(b.n)
+    cls = perfmodel.kernel_classes(b, q)
+    rng = np.random.default_rng(12)
+    keys = cls[:, 0] * 100 + cls[:, 1] * 10 + cls[:, 2]
+    sel = set(rng.choice(len(keys), 60, replace=False).tolist())
+    for key in np.unique(keys):
+        idx = np.nonzero(keys == key)[0]
+        sel.update(rng.choice(idx, min(8, idx.size), replace=False).tolist())
+    sel = np.array(sorted(sel))
+    sub = [np.ascontiguousarray(a[sel]) for a in q]
+    with api.Context(0) as ctx:
+        ctx.set_basis(b)
+        ctx.set_quartets(*sub)
+        gp = ctx.precond()
+        g, _ = ctx.gauss_eri()
+    ob = O.OracleBasis(b)
+    pairs = sorted({(int(i), int(k)) for i, k in zip(sub[0], sub[2])} | {(int(j), int(l)) for j, l in zip(sub[1], sub[3])})
+    pi = np.array([p[0] for p in pairs], np.int32)
+    pk = np.array([p[1] for p in pairs], np.int32)
+    diag = O.gauss_list(ob, [pi, pi, pk, pk])  # the (ik|ik) these quartets need
+    pre = np.zeros((b.n, b.n))
+    pre[pi - 1, pk - 1] = diag
+    pre[pk - 1, pi - 1] = diag
+    np.testing.assert_allclose(gp[pi - 1, pk - 1], diag, rtol=RTOL, atol=0)
+    ref, _ = O.gauss_eri(ob, sub, pre.reshape(-1, order="F"))
+    i, j, k, l = [a - 1 for a in sub]
+    bound = RTOL * np.abs(ref) + RTOL * np.sqrt(np.abs(pre[i, k] * pre[j, l]))
+    ratio = np.abs(g - ref) / bound
+    print(f"\nrandom molecule (111 STOs): {sel.size} quartets of {len(keys)} vs oracle, "
+          f"{len(np.unique(keys))} kernel instances, worst |gpu-oracle|/gate {ratio.max():.3e}")
+    assert np.all(ratio <= 1.0), f"{(ratio > 1).sum()} quartets outside the gate, worst {ratio.max():.3g}"
