@@ -188,6 +188,23 @@ def serving_run(rate: float, duration: float, large: str, max_running: int, seed
     return out
 
 
+def batch_run(nsys: int, min_atoms: int, max_atoms: int, seed: int = 1, max_running: int = 8) -> dict:
+    """The batched workload: `nsys` seeded systems of the random-molecule rules with min..max
+    atoms (uneven sizes) in one basis, their analytic ERIs in one launch per kernel class, each
+    system's MC (to max sigma <= 1e-6 Ha) as its own concurrent job; latency of a system = batch
+    start to its result."""
+    from slater_stoch_gb300 import batch, configs
+    rng = np.random.default_rng(seed)
+    systems = [configs.random_molecule(int(rng.integers(1, 2 ** 31 - 1)),
+                                       natoms=int(rng.integers(min_atoms, max_atoms + 1)), box=4.0)
+               for _ in range(nsys)]
+    _, rep = batch.batch_two_e(systems, list(range(1, nsys + 1)), sigma_target=SIGMA_TARGET,
+                               max_running=max_running)
+    out = rep.summary()
+    out.update({"atoms_per_system": [min_atoms, max_atoms]})
+    return out
+
+
 def random_molecule_run(natoms: int, mol_seed: int, seed: int, rank: int, q: int) -> dict:
     """The large single-system workload: the seeded random molecule (12 atoms: 111 STOs,
     1.93e7 unique ERIs), one job to max sigma <= 1e-6 Ha (shared-walker split-BF16 estimator,
@@ -254,10 +271,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=WALKERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="h2o_26", choices=["h2o_26", "serve", "random"],
+    ap.add_argument("--workload", default="h2o_26", choices=["h2o_26", "serve", "random", "batch"],
                     help="serve: only the open-loop serving run; random: only the large random-molecule "
                          "job (each its own JSON line)")
     ap.add_argument("--natoms", type=int, default=12, help="random: atoms of the random molecule")
+    ap.add_argument("--systems", type=int, default=64, help="batch: number of systems")
+    ap.add_argument("--atoms", type=int, nargs=2, default=[1, 3], help="batch: min and max atoms per system")
     ap.add_argument("--mol-seed", type=int, default=1, help="random: seed of the random molecule")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: arrivals per second")
     ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
@@ -272,6 +291,12 @@ def main():
     if args.workload == "random":
         line = {"metric": "unique ERIs/s at sigma<=1e-6 Ha, one large system (seeded random molecule)",
                 "workload": "random", "random": random_molecule_run(args.natoms, args.mol_seed, 1, 512, 4)}
+        print(json.dumps(line))
+        return
+    if args.workload == "batch":
+        line = {"metric": "unique ERIs/s and per-system p50/p99 latency, many systems in one batched launch",
+                "workload": "batch", "batch": batch_run(args.systems, args.atoms[0], args.atoms[1],
+                                                        max_running=args.max_running)}
         print(json.dumps(line))
         return
     if args.workload == "serve":

@@ -3,7 +3,7 @@
 // GB300 runs FP64 at about 1/64 of its FP32 rate (two DFMA per clock per SM), so a one-SM
 // solver of an n = 351 eigenproblem would take tens of milliseconds however it is written.
 // The routines here spread the FP64 work over the whole GPU:
-//  * dgemm: 64 x 64 output tiles, 256 threads with 4 x 4 accumulators each, 16-deep k steps
+//  * dgemm: 32 x 32 output tiles, 256 threads with 2 x 2 accumulators each, 16-deep k steps
 //    through shared memory; an inner dimension much longer than the output is split over
 //    CTAs into a workspace and summed in a fixed order (no atomics: reproducible results);
 //  * ortho_qr: blocked Householder QR (LAPACK's dgeqrf/dorgqr structure): one CTA factorises
@@ -43,8 +43,11 @@ unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 // ---------------------------------------------------------------------------------------
 // GEMM
 // ---------------------------------------------------------------------------------------
-constexpr int GT = 64, GKS = 16;
+constexpr int GT = 32, GKS = 16;
 
+// 32 x 32 output tile, 256 threads with 2 x 2 accumulators each (one FP64 FMA per shared-memory
+// read pair: FP64 throughput, not shared-memory bandwidth, is the limit).  Small tiles waste
+// little on the skinny products of the eigensolvers and Davidson (n = 10 columns).
 __global__ void __launch_bounds__(256) dgemm_kernel(int ta, int tb, int m, int n, int k, int kper, double alpha,
                                                     const double* __restrict__ A, int lda,
                                                     const double* __restrict__ B, int ldb, double beta,
@@ -54,11 +57,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int ta, int tb, int m, int n
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
   const int kb = blockIdx.z * kper, ke = min(k, kb + kper);
-  double acc[4][4];
-#pragma unroll
-  for (int r = 0; r < 4; r++)
-#pragma unroll
-    for (int c = 0; c < 4; c++) acc[r][c] = 0.0;
+  double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
   for (int k0 = kb; k0 < ke; k0 += GKS) {
     for (int e = threadIdx.x; e < GT * GKS; e += 256) {
       // consecutive threads along the contiguous dimension of the source
@@ -74,22 +73,19 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int ta, int tb, int m, int n
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GKS; kk++) {
-      double a[4], b[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) a[r] = As[kk][tx + 16 * r];
-#pragma unroll
-      for (int c = 0; c < 4; c++) b[c] = Bs[kk][ty + 16 * c];
-#pragma unroll
-      for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+      const double a0 = As[kk][tx], a1 = As[kk][tx + 16];
+      const double b0 = Bs[kk][ty], b1 = Bs[kk][ty + 16];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int r = 0; r < 4; r++)
+  for (int r = 0; r < 2; r++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
+    for (int c = 0; c < 2; c++) {
       const int gi = i0 + tx + 16 * r, gj = j0 + ty + 16 * c;
       if (gi >= m || gj >= n) continue;
       if (gridDim.z == 1) {
@@ -111,10 +107,11 @@ __global__ void dgemm_reduce(int m, int n, int ks, double alpha, const double* _
   *cp = beta == 0.0 ? alpha * s : fma(alpha, s, beta * *cp);
 }
 
+// K split so that the grid has about two CTAs per SM, each K slice at least 32 deep
 static void dgemm_split(int m, int n, int k, int* ks, int* kper) {
   const int64_t tiles = (int64_t)((m + GT - 1) / GT) * ((n + GT - 1) / GT);
   const int64_t target = 2 * (int64_t)sm_count();
-  int s = (int)std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (k + 63) / 64));
+  int s = (int)std::max<int64_t>(1, std::min<int64_t>((target + tiles - 1) / tiles, (k + 31) / 32));
   int per = (k + s - 1) / s;
   per = (per + GKS - 1) / GKS * GKS;
   *kper = std::max(per, GKS);
@@ -600,6 +597,7 @@ struct JacobiCtl {
   unsigned int count, gen;  // grid barrier
   int rot[2];               // rotations of the current / previous sweep (by sweep parity)
   double amax;
+  int sweeps;               // sweeps the last solve took
 };
 
 // Sense-free generation barrier over all CTAs of a cooperative launch (all co-resident).  A
@@ -678,8 +676,9 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
   if (!grid_barrier(ctl, err)) return;
   double* cur = A0;
   double* nxt = A1;
-  int converged = 0;
+  int converged = 0, sweeps_done = 0;
   for (int sweep = 0; sweep < JACOBI_MAX_SWEEPS && !converged; sweep++) {
+    sweeps_done = sweep + 1;
     for (int round = 0; round < np2 - 1; round++) {
       if (threadIdx.x == 0) s_rot = 0;
       if (round == 1 && blockIdx.x == 0 && threadIdx.x == 0) ctl->rot[(sweep + 1) & 1] = 0;
@@ -791,6 +790,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
     }
     converged = (*(volatile int*)&ctl->rot[sweep & 1] == 0);
   }
+  if (gtid == 0) ctl->sweeps = sweeps_done;
   if (!converged) {
     if (gtid == 0) atomicExch(err, 1);
     return;
