@@ -97,40 +97,69 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------
 # CPU baseline: the oracle (restated reference) on bounded samples of the workload
 # ------------------------------------------------------------------------------------------
-def cpu_baseline(b, q, budget_s: float = 20.0):
+def _class_keys(b, quartets):
+    from slater_stoch_gb300.perfmodel import kernel_classes
+    c = kernel_classes(b, quartets)
+    return c[:, 0] * 100 + c[:, 1] * 10 + c[:, 2]
+
+
+def _sampled_seconds(O, ob, quartets, keys, rng, per_class, cores):
+    """Estimated wall seconds of gauss_ijkl over every listed quartet on `cores` threads: a sample
+    stratified by kernel class (L, LK, tc) runs on all threads at once, each quartet timed on the
+    thread that computed it, and each class's sampled seconds are scaled by the class's
+    primitive-quartet count (the cost per primitive quartet differs several-fold between
+    classes; the quartets are independent, so the job divides over the cores)."""
+    qa = [np.asarray(a) for a in quartets]
+    sel = []
+    for key in np.unique(keys):
+        idx = np.nonzero(keys == key)[0]
+        sel.extend(rng.choice(idx, min(per_class, idx.size), replace=False).tolist())
+    sel = np.array(sorted(sel))
+    _, sec = O.gauss_list_timed(ob, [np.ascontiguousarray(a[sel]) for a in qa], cores)
+    total, sub_all, all_all = 0.0, 0.0, 0.0
+    for key in np.unique(keys):
+        idx = np.nonzero(keys == key)[0]
+        m = keys[sel] == key
+        cls_prims = O.count_primitive_quartets(ob, [np.ascontiguousarray(a[idx]) for a in qa])
+        sub_prims = O.count_primitive_quartets(ob, [np.ascontiguousarray(a[sel[m]]) for a in qa])
+        total += sec[m].sum() * cls_prims / max(sub_prims, 1.0)
+        sub_all += sub_prims
+        all_all += cls_prims
+    return total / cores, len(sel), sub_all, all_all
+
+
+def cpu_baseline(b, q, seed: int = 0, per_class: int = 4):
+    """One bounded sample of the job on the host cores, scaled to the whole job: the Schwarz
+    diagonal and the unique quartets each from a sample stratified by kernel class, the faithful
+    ZV-MC on 4,000 walkers (its cost is exactly proportional to the walker count)."""
     from oracle import binding as O
     ob = O.OracleBasis(b)
     nint = len(q[0])
     cores = os.cpu_count() or 1
-    rng = np.random.default_rng(0)
-    # analytic stage: a random subset of quartets, scaled by primitive-quartet count
-    total_prims = O.count_primitive_quartets(ob, q)
-    t = time.perf_counter()
-    pre = O.precond(ob, cores)
-    t_pre = time.perf_counter() - t
-    sel = rng.choice(nint, size=64, replace=False)
-    sub = tuple(np.ascontiguousarray(a[sel]) for a in q)
-    sub_prims = O.count_primitive_quartets(ob, sub)
-    t = time.perf_counter()
-    O.gauss_eri(ob, sub, pre, cores)
-    t_sub = time.perf_counter() - t
-    t_analytic = t_pre + t_sub * total_prims / sub_prims
-    # MC stage: faithful estimator (reference algorithm) on a bounded walker sample
+    rng = np.random.default_rng(seed)
+    n = b.n
+    di = np.array([i for i in range(1, n + 1) for k in range(1, i + 1)], np.int32)
+    dk = np.array([k for i in range(1, n + 1) for k in range(1, i + 1)], np.int32)
+    dq = [di, di, dk, dk]
+    t_pre, n_pre, _, _ = _sampled_seconds(O, ob, dq, _class_keys(b, dq), rng, max(per_class - 1, 1), cores)
+    t_eri, n_eri, sub_prims, total_prims = _sampled_seconds(O, ob, q, _class_keys(b, q), rng, per_class, cores)
     npts = 40 * 100
-    r = np.random.default_rng(1)
+    r = np.random.default_rng(1000 + seed)
     r1 = r.standard_normal((npts, 3))
     r2 = r.standard_normal((npts, 3))
     t = time.perf_counter()
     O.zvmc_faithful(ob, q, A_ZV, r1, r2, 1, npts, "ref32", nthreads=cores)
     t_mc_sample = time.perf_counter() - t
     t_mc = t_mc_sample * WALKERS / npts
+    t_analytic = t_pre + t_eri
     job = t_analytic + t_mc
     return {
         "value": nint / job, "unit": "ERIs/s", "cores": cores, "kind": "port",
-        "sample": (f"oracle (C restatement of the reference, OpenMP {cores} threads): Schwarz diagonal "
-                   f"in full ({t_pre:.1f}s) + 64 random quartets ({sub_prims:.3g} of {total_prims:.3g} "
-                   f"primitive quartets, {t_sub:.1f}s) scaled by primitive-quartet count; faithful "
-                   f"ZV-MC (ref32 casts) on {npts} walkers ({t_mc_sample:.1f}s) scaled to {WALKERS}"),
+        "sample": (f"oracle (C restatement of the reference, OpenMP {cores} threads): Schwarz diagonal from "
+                   f"{n_pre} and unique quartets from {n_eri} quartets stratified by kernel class ({sub_prims:.3g} "
+                   f"of {total_prims:.3g} primitive quartets), each quartet timed on its thread and each class "
+                   f"scaled by its primitive-quartet count ({t_analytic:.0f} s estimated on {cores} cores); "
+                   f"faithful ZV-MC (ref32 casts) on {npts} walkers ({t_mc_sample:.2f} s) scaled to {WALKERS}"),
         "job_seconds_estimated": job, "analytic_s": t_analytic, "mc_s": t_mc,
     }
 
@@ -138,15 +167,16 @@ def cpu_baseline(b, q, budget_s: float = 20.0):
 def run_reference(args):
     """The reference's algorithm on the host cores (the C oracle restatement, OpenMP on all
     cores; the Fortran reference cannot be built here).  Each step is one bounded sample of the
-    job (full Schwarz diagonal, 64 random quartets, 4,000 faithful walkers) scaled to the whole
-    job; W untimed steps, then K timed ones; value = ERIs per estimated job second."""
+    job (Schwarz-diagonal and unique quartets stratified by kernel class, 4,000 faithful walkers)
+    scaled to the whole job, a different sample each step; W untimed steps, then K timed ones;
+    value = ERIs per estimated job second."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     b, q = _workload()
-    for _ in range(args.warmup):
-        cpu_baseline(b, q)
-    steps = [cpu_baseline(b, q) for _ in range(max(args.steps, 1))]
+    for w in range(args.warmup):
+        cpu_baseline(b, q, seed=1000 + w, per_class=2)
+    steps = [cpu_baseline(b, q, seed=s, per_class=2) for s in range(max(args.steps, 1))]
     job_s = statistics.mean(c["job_seconds_estimated"] for c in steps)
     nint = len(q[0])
     value = nint / job_s
@@ -169,19 +199,20 @@ def run_reference(args):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
-def serving_run(rate: float, duration: float, large: str, max_running: int, seed: int = 1) -> dict:
+def serving_run(rate: float, duration: float, large: str, max_running: int, seed: int = 1,
+                max_atoms: int = 1) -> dict:
     """Open-loop Poisson serving run (slater_stoch_gb300.serving): requests arrive at `rate`
-    per second for `duration` seconds, each a small random system (1-2 atoms of the random-
-    molecule rules, 4-22 STOs) or with probability 0.05 the `large` system, with error-bar
-    targets log-uniform in [1e-7, 1e-5] Ha; admitted within a 150 GB ERI budget and
-    `max_running` concurrent jobs, each retired at its target."""
+    per second for `duration` seconds, each a small random system (1..max_atoms atoms of the
+    random-molecule rules: 4 or 11 STOs for one atom) or with probability 0.05 the `large`
+    system, with error-bar targets log-uniform in [1e-7, 1e-5] Ha; admitted within a 150 GB ERI
+    budget and `max_running` concurrent jobs, each retired at its target."""
     from slater_stoch_gb300 import configs, serving
     big = getattr(configs, large)(ng0=20)
-    reqs = serving.make_requests(seed, rate, duration, large=big)
+    reqs = serving.make_requests(seed, rate, duration, large=big, max_atoms=max_atoms)
     t = time.perf_counter()
     rep = serving.serve(reqs, max_running=max_running)
     out = rep.summary()
-    out.update({"rate_per_s": rate, "duration_s": duration, "large_system": large,
+    out.update({"rate_per_s": rate, "duration_s": duration, "large_system": large, "max_atoms": max_atoms,
                 "requests": len(reqs), "max_running": max_running,
                 "sizes_nbasis": [int(min(r.basis.n for r in reqs)), int(max(r.basis.n for r in reqs))],
                 "elapsed_s": time.perf_counter() - t})
@@ -282,6 +313,7 @@ def main():
     ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
     ap.add_argument("--large", default="h2o_minimal", help="serving: the 5%% large system")
     ap.add_argument("--max-running", type=int, default=8, help="serving: concurrent jobs")
+    ap.add_argument("--max-atoms", type=int, default=1, help="serving: atoms per small system")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--fp32-eps", type=float, default=None,
                     help="FP32-tier threshold of the analytic stage (ss_set_eri_tiers); default: the library's")
@@ -301,7 +333,8 @@ def main():
         return
     if args.workload == "serve":
         line = {"metric": "unique ERIs/s under open-loop Poisson arrivals; p50/p99 job latency",
-                "workload": "serve", "serving": serving_run(args.rate, args.duration, args.large, args.max_running)}
+                "workload": "serve", "serving": serving_run(args.rate, args.duration, args.large, args.max_running,
+                                               max_atoms=args.max_atoms)}
         print(json.dumps(line))
         return
 
@@ -473,7 +506,8 @@ def main():
         }
         if world == 1 and not args.no_serving:
             try:
-                line["serving"] = serving_run(args.rate, min(args.duration, 10.0), args.large, args.max_running)
+                line["serving"] = serving_run(args.rate, min(args.duration, 10.0), args.large, args.max_running,
+                                              max_atoms=args.max_atoms)
             except Exception as ex:  # reported, not fatal for the throughput line
                 line["serving"] = {"error": str(ex)}
         if world == 1 and not args.no_cpu_baseline:

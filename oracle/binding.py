@@ -52,6 +52,9 @@ def lib():
                                     f64p, C.c_int]
         L.orc_gauss_list.restype = None
         L.orc_gauss_list.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p, i32p, i32p, f64p, C.c_int]
+        L.orc_gauss_list_timed.restype = None
+        L.orc_gauss_list_timed.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p, i32p, i32p, f64p, f64p,
+                                           C.c_int]
         L.orc_count_primitive_quartets.restype = C.c_double
         L.orc_count_primitive_quartets.argtypes = [C.POINTER(OrcBasis), C.c_int64, i32p, i32p,
                                                    i32p, i32p]
@@ -149,6 +152,15 @@ def gauss_list(ob: OracleBasis, quartets, nthreads=0):
     out = np.zeros(len(q[0]))
     lib().orc_gauss_list(C.byref(ob.s), len(q[0]), *q, out, _threads(nthreads))
     return out
+
+
+def gauss_list_timed(ob: OracleBasis, quartets, nthreads=0):
+    """gauss_list plus each quartet's own seconds on the thread that computed it."""
+    q = [np.ascontiguousarray(a, np.int32) for a in quartets]
+    out = np.zeros(len(q[0]))
+    sec = np.zeros(len(q[0]))
+    lib().orc_gauss_list_timed(C.byref(ob.s), len(q[0]), *q, out, sec, _threads(nthreads))
+    return out, sec
 
 
 def count_primitive_quartets(ob: OracleBasis, quartets):

@@ -20,6 +20,7 @@
 #include "ss_oracle.h"
 
 #include <math.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -714,6 +715,26 @@ void orc_gauss_list(const orc_basis *b, int64_t nint, const int32_t *is, const i
 #endif
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t q = 0; q < nint; q++) out[q] = orc_gauss_ijkl(b, is[q] - 1, ks[q] - 1, js[q] - 1, ls[q] - 1);
+}
+
+/* the same, with the seconds each quartet took on the thread that computed it (seconds may be
+ * NULL); quartets are handed out one at a time, so a sample of quartets from several classes
+ * runs on all threads at once and each quartet's time is its own single-thread cost */
+void orc_gauss_list_timed(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                          const int32_t *ks, const int32_t *ls, double *out, double *seconds, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t q = 0; q < nint; q++) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    out[q] = orc_gauss_ijkl(b, is[q] - 1, ks[q] - 1, js[q] - 1, ls[q] - 1);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (seconds) seconds[q] = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+  }
 }
 
 /* ------------------------------------------------------------------ */

@@ -71,6 +71,8 @@ int64_t orc_gauss_eri(const orc_basis *b, int64_t nint, const int32_t *is, const
                       double *out, int nthreads);
 void orc_gauss_list(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
                     const int32_t *ks, const int32_t *ls, double *out, int nthreads);
+void orc_gauss_list_timed(const orc_basis *b, int64_t nint, const int32_t *is, const int32_t *js,
+                          const int32_t *ks, const int32_t *ls, double *out, double *seconds, int nthreads);
 
 /* primitive-quartet count of the sweep (sum over quartets of prod n_gauss*nc) */
 double orc_count_primitive_quartets(const orc_basis *b, int64_t nint, const int32_t *is,
