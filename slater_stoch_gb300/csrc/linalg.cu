@@ -203,11 +203,11 @@ __device__ __forceinline__ void hypot_inv(double f, double g, double& r, double&
 // Panel j0 .. j0+b-1 of Z (rows j0 .. N-1): Householder vectors in place below the diagonal
 // (unit leading entry implied), and explicitly into Vb(:, j0 .. j0+b-1) (zeros above, 1 on the
 // diagonal); T (QR_NB x QR_NB col-major, upper triangular) with H_j0 ... H_{j0+b-1} =
-// I - V T V^T (the forward column-wise recurrence of LAPACK's dlarft).  1024 threads.  With
+// I - V T V^T (the forward column-wise recurrence of LAPACK's dlarft).  256 threads.  With
 // SMEM the panel's mr = N - j0 rows are staged in shared memory (mr x b doubles), so the
 // column-by-column steps read no global memory; otherwise it is factorised in place.
 template <bool SMEM>
-__global__ void __launch_bounds__(1024) qr_panel_kernel(int N, int j0, int b, double* __restrict__ Z, int ld,
+__global__ void __launch_bounds__(256) qr_panel_kernel(int N, int j0, int b, double* __restrict__ Z, int ld,
                                                         double* __restrict__ Vb, double* __restrict__ T) {
   extern __shared__ double s_panel[];
   __shared__ double sh[32];
@@ -347,9 +347,9 @@ int ortho_qr(cudaStream_t st, int N, int r, double* Z, int ld, double* work, int
     if (psmem <= QR_PANEL_SMEM_MAX) {
       SS_CUDA_TRY(cudaFuncSetAttribute(qr_panel_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)QR_PANEL_SMEM_MAX));
-      qr_panel_kernel<true><<<1, 1024, psmem, st>>>(N, j0, b, Z, ld, Vb, Tp);
+      qr_panel_kernel<true><<<1, 256, psmem, st>>>(N, j0, b, Z, ld, Vb, Tp);
     } else {
-      qr_panel_kernel<false><<<1, 1024, 0, st>>>(N, j0, b, Z, ld, Vb, Tp);
+      qr_panel_kernel<false><<<1, 256, 0, st>>>(N, j0, b, Z, ld, Vb, Tp);
     }
     SS_CUDA_TRY(cudaGetLastError());
     if (launches) (*launches)++;
@@ -386,7 +386,7 @@ int ortho_qr(cudaStream_t st, int N, int r, double* Z, int ld, double* work, int
 // ---------------------------------------------------------------------------------------
 constexpr int EIG_SMEM_MAX = 128;
 
-__global__ void __launch_bounds__(1024) sym_eig_smem_kernel(int n, const double* __restrict__ Ain,
+__global__ void __launch_bounds__(256) sym_eig_smem_kernel(int n, const double* __restrict__ Ain,
                                                             double* __restrict__ Vout, double* __restrict__ w,
                                                             int* __restrict__ err) {
   extern __shared__ double s_dyn[];
@@ -667,7 +667,9 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
   double* ss = sc + np;
   const double eps = 2.2204460492503131e-16;
   const double amax = ctl->amax;
-  const double tiny = 0.1 * eps * amax;  // rounding level of the matrix entries
+  // entries at or below the rounding level of the matrix (eps max|A|): rounding in the other
+  // rotations of their rows regenerates them at that size, so rotating them would never end
+  const double tiny = eps * amax;
   const double inv_amax = amax > 0.0 ? 1.0 / amax : 0.0;
   const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -721,7 +723,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int n, double* __restrict__
       // A' = J^T A J by 2 x 2 blocks (pair P rows, pair R columns), P <= R; block (R, P) is
       // the transpose, written from the same values so the matrix stays exactly symmetric
       for (int64_t it = gtid; it < (int64_t)np * (np + 1) / 2; it += gthreads) {
-        int R = (int)((sqrt(8.0 * (double)it + 1.0) - 1.0) * 0.5);
+        int R = (int)((sqrtf(8.0f * (float)it + 1.0f) - 1.0f) * 0.5f);  // corrected below
         while ((int64_t)R * (R + 1) / 2 > it) R--;
         while ((int64_t)(R + 1) * (R + 2) / 2 <= it) R++;
         const int P = (int)(it - (int64_t)R * (R + 1) / 2);
@@ -832,7 +834,9 @@ int sym_eig(cudaStream_t st, int n, const double* A, double* V, double* w, doubl
     // different sizes at once never lower it under another's launch
     const int smem_max = (int)(sizeof(double) * (EIG_SMEM_MAX * EIG_SMEM_MAX + 5 * EIG_SMEM_MAX));
     SS_CUDA_TRY(cudaFuncSetAttribute(sym_eig_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
-    sym_eig_smem_kernel<<<1, 1024, smem, st>>>(n, A, V, w, d_err);
+    // 256 threads: eight warps keep the FP64 pipe busy, and each of the many block-wide
+    // barriers of the reduction gathers 8 warps instead of 32
+    sym_eig_smem_kernel<<<1, 256, smem, st>>>(n, A, V, w, d_err);
     SS_CUDA_TRY(cudaGetLastError());
     if (launches) (*launches)++;
     return SS_OK;
@@ -853,7 +857,8 @@ int sym_eig(cudaStream_t st, int n, const double* A, double* V, double* w, doubl
                                    (int)(sizeof(double) * 2 * ((4096 + 1) / 2))));  // the largest n
   int per_sm = 0;
   SS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_kernel, 256, smem));
-  const int64_t want = std::max<int64_t>(1, ((int64_t)np * (np + 1) / 2 + 255) / 256);
+  const int64_t items = std::max<int64_t>((int64_t)np * (np + 1) / 2, (int64_t)n * np);  // 2x2 blocks, V rows
+  const int64_t want = std::max<int64_t>(1, (items + 255) / 256);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * std::max(per_sm, 1)));
   int nn = n;
   void* args[] = {&nn, &A0, &A1, &Vu, &d, &ctl, &d_err};
