@@ -309,7 +309,7 @@ def main():
     ap.add_argument("--systems", type=int, default=64, help="batch: number of systems")
     ap.add_argument("--atoms", type=int, nargs=2, default=[1, 3], help="batch: min and max atoms per system")
     ap.add_argument("--mol-seed", type=int, default=1, help="random: seed of the random molecule")
-    ap.add_argument("--rate", type=float, default=20.0, help="serving: arrivals per second")
+    ap.add_argument("--rate", type=float, default=15.0, help="serving: arrivals per second")
     ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
     ap.add_argument("--large", default="h2o_minimal", help="serving: the 5%% large system")
     ap.add_argument("--max-running", type=int, default=8, help="serving: concurrent jobs")
@@ -464,13 +464,15 @@ def main():
 
     from slater_stoch_gb300.perfmodel import primitive_quartets
     nprim = primitive_quartets(b, q)
-    from slater_stoch_gb300.perfmodel import EXEC_FLOPS
+    from slater_stoch_gb300.perfmodel import EXEC_DRAM_BYTES, EXEC_FLOPS
     wl = f"{NINT_WORKLOAD}_ng20"
     flops = eri_fp64_flops(b, q, wl)
     peak64 = fp64_peak_tflops(torch)
     achieved = flops / t_analytic / 1e12 if flops else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                "frac": achieved / peak64 if (peak64 and achieved) else None, "traffic": None,
+                "frac": achieved / peak64 if (peak64 and achieved) else None,
+                "traffic": EXEC_DRAM_BYTES.get(wl),
+                "traffic_note": "DRAM bytes of all eri_kernel launches of one job (ncu, one pass per metric)",
                 "kernel": "eri_kernel (analytic Gaussian-fit ERIs, all launches of one job)",
                 "peak_source": "measured in this run: torch float64 matmul 4096^3 (FP64 peak is not "
                                "in MEASURED_PEAKS.json)",
@@ -510,6 +512,10 @@ def main():
                                               max_atoms=args.max_atoms)
             except Exception as ex:  # reported, not fatal for the throughput line
                 line["serving"] = {"error": str(ex)}
+            try:
+                line["batch"] = batch_run(16, 1, 2, max_running=args.max_running)
+            except Exception as ex:
+                line["batch"] = {"error": str(ex)}
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_baseline(b, q)
             line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

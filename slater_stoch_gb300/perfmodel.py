@@ -8,7 +8,8 @@
 * EXEC_FLOPS: executed flops of all eri_kernel launches of one job (Schwarz factors, Schwarz
   diagonal and screened quartets), from ncu instruction counters on the full workload
   (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd,ffma}_pred_on.sum, one pass each; DFMA
-  and FFMA counted as 2 flops).  Command and per-class table: profiles/eri_kernel_h2o26.md.
+  and FFMA counted as 2 flops), and EXEC_DRAM_BYTES their DRAM traffic.  Command and per-class
+  table: profiles/eri_kernel_h2o26.md.
 * EXEC_FLOPS_PER_PRIM: the earlier all-FP64 kernel's executed FP64 flops per primitive quartet
   (241.5, unscreened), kept as the model for workloads without a measurement.
 """
@@ -19,9 +20,16 @@ import numpy as np
 # executed FP64 flops per primitive quartet of the all-FP64 kernel (fallback model)
 EXEC_FLOPS_PER_PRIM = 241.5
 
-# workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job
+# workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job, at
+# the default tiers (primitive screen 1e-18, FP32 tier below 1e-11 of the Schwarz bound)
 EXEC_FLOPS = {
-    "h2o_26_ng20": (8.2948e11, 3.3580e11),
+    "h2o_26_ng20": (6.003e11, 4.777e11),
+}
+# workload -> DRAM bytes (read + write) of all eri_kernel launches of one job (ncu
+# dram__bytes_read.sum + dram__bytes_write.sum, one pass each; mostly the local-memory spill
+# traffic of the L = 4 classes with several r^2-type fits)
+EXEC_DRAM_BYTES = {
+    "h2o_26_ng20": 1.157e10,
 }
 
 
