@@ -315,6 +315,7 @@ def main():
     ap.add_argument("--max-running", type=int, default=8, help="serving: concurrent jobs")
     ap.add_argument("--max-atoms", type=int, default=1, help="serving: atoms per small system")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-cleanup", action="store_true", help="skip the cleanup section (profiling runs)")
     ap.add_argument("--fp32-eps", type=float, default=None,
                     help="FP32-tier threshold of the analytic stage (ss_set_eri_tiers); default: the library's")
     args = ap.parse_args()
@@ -435,6 +436,8 @@ def main():
     eri_final, _ = ctx.two_e_job(A_ZV, seed, npts, NBLOCKS, "shared", "split_bf16", 0.0, copy=True)
     cleanup = {"nonfinite_eris": int((~np.isfinite(eri_final)).sum())}
     try:  # reported, not fatal for the throughput line
+        if args.no_cleanup:
+            raise RuntimeError("skipped (--no-cleanup)")
         t = time.perf_counter()
         c1, n_svd = ctx.psd_clean(eri_final, layout="packed_pair", rank=200, oversample=10, q=4, seed=seed)
         t_svd = time.perf_counter() - t
