@@ -123,9 +123,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
                    const double* d_pre, double eps, double eps32, double* self_out = nullptr) {
   // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
-  // functions) and, for L >= 3, the light-ket variant v: the lighter pair has L <= v (v = 1, 2;
-  // v = 0 for the others).  A light-ket quartet is evaluated as (jl|ik) when (j,l) is the
-  // lighter pair (bit 62 of its work entry).  Bucket index 3 (5 L + tc) + v.
+  // functions) and the light-ket variant v: the lighter pair has L <= v (v = 1, 2 for L >= 3,
+  // v = 1 for L = 2; v = 0 for the others).  A light-ket quartet is evaluated as (jl|ik) when
+  // (j,l) is the lighter pair (bit 62 of its work entry).  Bucket index 3 (5 L + tc) + v.
   const int NB = 3 * 5 * (SS_MAX_POW + 1);
   const int64_t SWAP = int64_t(1) << 62;
   std::vector<std::vector<int64_t>> bucket(NB);
@@ -135,7 +135,7 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     int L = std::max(Lb, Lk);
     int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = (L >= 3 && lmin <= 2 && !self_out) ? std::max(lmin, 1) : 0;
+    const int v = (!self_out && ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1))) ? std::max(lmin, 1) : 0;
     bucket[3 * (5 * L + nt) + v].push_back(v && Lk > Lb ? (t | SWAP) : t);
   }
   // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes

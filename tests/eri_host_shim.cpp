@@ -112,6 +112,8 @@ double quartet_value(const BasisDev& B, int fi, int fk, int fj, int fl, bool fol
   do {                                                             \
     if (LK < L) {                                                  \
       if (LK == 1) {                                               \
+        if (L == 2 && tc == 0) return F<2, 0, 1>(__VA_ARGS__);     \
+        if (L == 2 && tc == 1) return F<2, 1, 1>(__VA_ARGS__);     \
         if (L == 3 && tc == 0) return F<3, 0, 1>(__VA_ARGS__);     \
         if (L == 3 && tc == 1) return F<3, 1, 1>(__VA_ARGS__);     \
         if (L == 3 && tc == 2) return F<3, 2, 1>(__VA_ARGS__);     \
@@ -296,7 +298,7 @@ int ss_host_eri(int n, int ld, const double* center, const int* npower, const in
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = (mode == 0 && L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    const int v = (mode == 0 && ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1))) ? std::max(lmin, 1) : 0;
     const bool swp = (v && Lk > Lb) || mode == 2;
     if (swp) {
       std::swap(i, j);
@@ -326,7 +328,7 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = (L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    const int v = ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1)) ? std::max(lmin, 1) : 0;
     const double sch = std::sqrt(pre[i + (int64_t)n * k] * pre[j + (int64_t)n * l]);
     if (v && Lk > Lb) {
       std::swap(i, j);
@@ -384,7 +386,7 @@ int ss_host_tier_counts(int n, int ld, const double* center, const int* npower, 
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = (L >= 3 && lmin <= 2) ? std::max(lmin, 1) : 0;
+    const int v = ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1)) ? std::max(lmin, 1) : 0;
     cls[3 * q] = L;
     cls[3 * q + 1] = v ? v : L;
     cls[3 * q + 2] = tc;

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import eri_host
-from slater_stoch_gb300 import basis, configs
+from slater_stoch_gb300 import basis, configs, perfmodel
 
 HERE = Path(__file__).resolve().parent
 PRIM_FP32_EPS = 1e-11  # the kernel's default threshold of the FP32 tier (csrc/ss_common.cuh)
@@ -59,7 +59,10 @@ def h2o26(lib):
 def test_host_kernel_matches_oracle_h2o26(lib, h2o26):
     b, q, pre, ref = h2o26
     got, lk = _host_eri(lib, b, q, mode=0)
-    assert (lk == 1).sum() > 0 and (lk == 2).sum() > 0  # the light-ket instances are exercised
+    cls = perfmodel.kernel_classes(b, q)
+    assert (cls[:, 1] == lk).all()  # the Python classifier picks the instances the host build uses
+    for L, LK in ((2, 1), (3, 1), (3, 2), (4, 1), (4, 2)):  # every light-ket bound is exercised
+        assert ((cls[:, 0] == L) & (lk == LK)).sum() > 0, (L, LK)
     ok = _gate(got, ref, pre, q, b.n)
     assert ok.all(), f"{(~ok).sum()} quartets outside the gate"
 
