@@ -193,6 +193,11 @@ cudaError_t launch_eri_L3c2(dim3, int, size_t, cudaStream_t, const BasisDev&, co
 cudaError_t launch_eri_L4c2(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c3(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L4c4(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L1c0k0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c0k0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L2c1k0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c0k0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
+cudaError_t launch_eri_L3c1k0(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L2c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L2c1k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
 cudaError_t launch_eri_L3c0k1(dim3, int, size_t, cudaStream_t, const BasisDev&, const PrimPair*, const int64_t*, const int*, const int64_t*, int, const int32_t*, const int32_t*, const int32_t*, const int32_t*, const double*, double, double, double*, double*, const PrimPairF*);
@@ -211,9 +216,9 @@ cudaError_t launch_eri_L4c3k2(dim3, int, size_t, cudaStream_t, const BasisDev&, 
 
 // Kernel instance for class (L, tc) and ket bound LK.  tc: number of r^2-type fits among the
 // four functions (0..4).  A quartet with r^2-type fits has L >= 2, and one with three or four has
-// L = 4; an instance with a larger L serves any smaller one (degrees are runtime).  LK = 1, 2 < L
-// (L = 3, 4) and LK = 1 < L = 2: the light-ket instances (a ket with L <= 1 holds no r^2-type
-// fit, one with L = 2 at most one, so tc <= 1 for L = 2, tc <= 2 and tc <= 3 for L = 3, 4).
+// L = 4; an instance with a larger L serves any smaller one (degrees are runtime).  LK < L: the
+// light-ket instances of ss_light_ket (a ket with L <= 1 holds no r^2-type fit, one with L = 2 at
+// most one; a bra with L <= 3 at most one, with L = 4 at most two).
 cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t smem, cudaStream_t st,
                              const BasisDev& B, const PrimPair* pp, const int64_t* off, const int* cnt,
                              const int64_t* work, int split, const int32_t* is, const int32_t* js,
@@ -224,6 +229,7 @@ cudaError_t launch_eri_class(int L, int LK, int tc, dim3 grid, int ktile, size_t
   if (L == LL && tc == TT && LK == KK)                                                                          \
     return launch_eri_L##LL##c##TT##k##KK(grid, ktile, smem, st, B, pp, off, cnt, work, split, is, js, ks, ls, \
                                           pre, eps, eps32, partial, self_out, ppf);
+    SS_KV(1, 0, 0) SS_KV(2, 0, 0) SS_KV(2, 1, 0) SS_KV(3, 0, 0) SS_KV(3, 1, 0)
     SS_KV(2, 0, 1) SS_KV(2, 1, 1)
     SS_KV(3, 0, 1) SS_KV(3, 1, 1) SS_KV(3, 2, 1) SS_KV(4, 0, 1) SS_KV(4, 1, 1) SS_KV(4, 2, 1)
     SS_KV(3, 0, 2) SS_KV(3, 1, 2) SS_KV(3, 2, 2) SS_KV(4, 0, 2) SS_KV(4, 1, 2) SS_KV(4, 2, 2) SS_KV(4, 3, 2)

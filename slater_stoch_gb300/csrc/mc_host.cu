@@ -209,6 +209,12 @@ static int run_faithful(ss_ctx* c, double a_zv, uint64_t seed, const double* hr1
   return SS_OK;
 }
 
+static int cuda_rc(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return SS_OK;
+  ss_set_cuda_error(e, what, __FILE__, __LINE__);
+  return SS_ERR_CUDA;
+}
+
 static int copy_out(ss_ctx* c, double* mean, double* sigma) {
   if (mean)
     CUTRY(cudaMemcpyAsync(mean, c->d_mean.ptr, sizeof(double) * c->nint, cudaMemcpyDeviceToHost, c->stream));
@@ -315,8 +321,37 @@ int ss_two_e_job(ss_ctx* c, double a_zv, uint64_t seed, int64_t samples_per_bloc
                  int precision, double sigma_target, double* eri, double* sigma) {
   SS_CTX(c);
   c->have_precond = c->have_gauss = c->have_mc = false;
-  TRY(ensure_gauss(c));
-  TRY(ss_zvmc(c, a_zv, seed, samples_per_block, nblocks, estimator, precision, sigma_target, nullptr, nullptr));
+  // The analytic stage and the MC meet only in ss_combine.  The analytic stage is queued on its
+  // own lowest-priority stream (ensure_gauss returns once its launches are queued) and the MC
+  // runs on the context stream (greatest priority) meanwhile: the MC kernels take SM slots as
+  // ERI CTAs retire instead of waiting for the whole stage (measured on the 26-function H2O job:
+  // 1.771 s -> 1.740 s; without the priorities the two streams gave no gain).  Results are
+  // bitwise the same.  The context stream waits for the analytic stage before the combine.
+  if (!c->ana_stream) {
+    int lo = 0, hi = 0;
+    SS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    SS_CUDA_TRY(cudaStreamCreateWithPriority(&c->ana_stream, cudaStreamNonBlocking, lo));
+    SS_CUDA_TRY(cudaEventCreateWithFlags(&c->ana_fork, cudaEventDisableTiming));
+    SS_CUDA_TRY(cudaEventCreateWithFlags(&c->ana_done, cudaEventDisableTiming));
+  }
+  SS_CUDA_TRY(cudaEventRecord(c->ana_fork, c->stream));  // after the basis and quartet uploads
+  SS_CUDA_TRY(cudaStreamWaitEvent(c->ana_stream, c->ana_fork, 0));
+  cudaStream_t ctx_stream = c->stream;
+  c->stream = c->ana_stream;
+  int rc = ensure_gauss(c);
+  if (!rc) rc = cuda_rc(cudaEventRecord(c->ana_done, c->ana_stream), "cudaEventRecord");
+  c->stream = ctx_stream;
+  if (rc) {
+    cudaStreamSynchronize(c->ana_stream);
+    return rc;
+  }
+  rc = ss_zvmc(c, a_zv, seed, samples_per_block, nblocks, estimator, precision, sigma_target, nullptr, nullptr);
+  // the join is queued on every path, so no analytic work outlives the call unobserved
+  const int jrc = cuda_rc(cudaStreamWaitEvent(c->stream, c->ana_done, 0), "cudaStreamWaitEvent");
+  if (rc || jrc) {
+    cudaStreamSynchronize(c->ana_stream);
+    return rc ? rc : jrc;
+  }
   TRY(ss_combine(c, eri));
   if (sigma) TRY(copy_out(c, nullptr, sigma));
   return SS_OK;

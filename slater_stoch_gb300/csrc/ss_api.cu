@@ -104,6 +104,24 @@ int h2d(ss_ctx* c, DevBuf& b, const void* src, size_t bytes) {
   return SS_OK;
 }
 
+int h2d_async(ss_ctx* c, DevBuf& b, const void* src, size_t bytes) {
+  int rc = dev_alloc(c, b, bytes);
+  if (rc) return rc;
+  if (!c->pin_evt) SS_CUDA_TRY(cudaEventCreateWithFlags(&c->pin_evt, cudaEventDisableTiming));
+  SS_CUDA_TRY(cudaEventSynchronize(c->pin_evt));  // the previous copy has left the buffer
+  if (c->pin_cap < bytes) {
+    if (c->pin) SS_CUDA_TRY(cudaFreeHost(c->pin));
+    c->pin = nullptr;
+    c->pin_cap = 0;
+    SS_CUDA_TRY(cudaHostAlloc(&c->pin, bytes, cudaHostAllocDefault));
+    c->pin_cap = bytes;
+  }
+  memcpy(c->pin, src, bytes);
+  SS_CUDA_TRY(cudaMemcpyAsync(b.ptr, c->pin, bytes, cudaMemcpyHostToDevice, c->stream));
+  SS_CUDA_TRY(cudaEventRecord(c->pin_evt, c->stream));
+  return SS_OK;
+}
+
 // per-axis maximum of (power of f1 + power of f2) over the cartesian components of the fits
 static int pair_L(const ss_ctx* c, int f1, int f2) {
   int L = 0;
@@ -123,10 +141,10 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
                    const std::vector<int64_t>& sel, std::vector<int64_t>& slot_of_sel, int64_t& npartial,
                    const double* d_pre, double eps, double eps32, double* self_out = nullptr) {
   // bucket by class (L = max(bra L, ket L), tc = number of r^2-type fits among the four
-  // functions) and the light-ket variant v: the lighter pair has L <= v (v = 1, 2 for L >= 3,
-  // v = 1 for L = 2; v = 0 for the others).  A light-ket quartet is evaluated as (jl|ik) when
-  // (j,l) is the lighter pair (bit 62 of its work entry).  Bucket index 3 (5 L + tc) + v.
-  const int NB = 3 * 5 * (SS_MAX_POW + 1);
+  // functions) and the ket bound of the light-ket rule (ss_light_ket): v = LK + 1, or 0 for the
+  // full-L instance.  A light-ket quartet is evaluated as (jl|ik) when (j,l) is the lighter pair
+  // (bit 62 of its work entry).  Bucket index 4 (5 L + tc) + v.
+  const int NB = 4 * 5 * (SS_MAX_POW + 1);
   const int64_t SWAP = int64_t(1) << 62;
   std::vector<std::vector<int64_t>> bucket(NB);
   for (int64_t t : sel) {
@@ -134,9 +152,8 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
     const int Lb = pair_L(c, i, k), Lk = pair_L(c, j, l);
     int L = std::max(Lb, Lk);
     int nt = (c->h_itype[i] == 2) + (c->h_itype[k] == 2) + (c->h_itype[j] == 2) + (c->h_itype[l] == 2);
-    const int lmin = std::min(Lb, Lk);
-    const int v = (!self_out && ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1))) ? std::max(lmin, 1) : 0;
-    bucket[3 * (5 * L + nt) + v].push_back(v && Lk > Lb ? (t | SWAP) : t);
+    const int v = self_out ? 0 : ss_light_ket(L, std::min(Lb, Lk)) + 1;
+    bucket[4 * (5 * L + nt) + v].push_back(v && Lk > Lb ? (t | SWAP) : t);
   }
   // Each class is split into enough bra slices that its launch has ~8 CTAs per SM (classes
   // with few quartets, such as the Schwarz diagonal's or the four-r^2-fit class, up to 127 ways,
@@ -177,8 +194,10 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   // classes launched round-robin over the side streams, largest launch first; the side streams
   // start after everything queued on the context stream and the context stream waits for all
   if (!c->eri_fork) {
+    int lo = 0, hi = 0;  // lowest priority: the MC of a job runs beside the analytic stage
+    SS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     for (int s = 0; s < ss_ctx::ERI_STREAMS; s++) {
-      SS_CUDA_TRY(cudaStreamCreateWithFlags(&c->eri_stream[s], cudaStreamNonBlocking));
+      SS_CUDA_TRY(cudaStreamCreateWithPriority(&c->eri_stream[s], cudaStreamNonBlocking, lo));
       SS_CUDA_TRY(cudaEventCreateWithFlags(&c->eri_join[s], cudaEventDisableTiming));
     }
     SS_CUDA_TRY(cudaEventCreateWithFlags(&c->eri_fork, cudaEventDisableTiming));
@@ -194,9 +213,9 @@ static int run_eri(ss_ctx* c, const int32_t* d_qis, const int32_t* d_qjs, const 
   for (size_t oi = 0; oi < order.size() && !launch_rc; oi++) {
     const int bk = order[oi];
     cudaStream_t st = c->eri_stream[oi % ss_ctx::ERI_STREAMS];
-    const int L = (bk / 3) / 5;
-    const int tc = (bk / 3) % 5;
-    const int LK = (bk % 3) ? bk % 3 : L;
+    const int L = (bk / 4) / 5;
+    const int tc = (bk / 4) % 5;
+    const int LK = (bk % 4) ? bk % 4 - 1 : L;
     const bool t2 = tc > 0;
     int ktile;
     size_t smem;
@@ -362,7 +381,7 @@ int ensure_gauss(ss_ctx* c) {
                (const int32_t*)c->d_ls.ptr, c->h_is, c->h_js, c->h_ks, c->h_ls, sel, slot, npartial,
                (const double*)c->d_precond.ptr, c->eri_eps_screen, c->eri_eps32);
   if (rc) return rc;
-  rc = h2d(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
+  rc = h2d_async(c, c->d_scratch_c, slot.data(), sizeof(int64_t) * c->nint);
   if (rc) return rc;
   rc = dev_alloc(c, c->d_gauss, sizeof(double) * c->nint);
   if (rc) return rc;
@@ -440,7 +459,12 @@ ss_ctx* ss_create(int device, size_t hbm_budget) {
   c->budget = hbm_budget;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (c->num_sms <= 0) c->num_sms = 152;
-  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  {  // the context stream has the greatest priority: in ss_two_e_job the MC kernels queued on it
+     // take SM slots as the analytic stage's (lowest-priority) CTAs retire
+    int lo = 0, hi = 0;
+    e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, hi);
+  }
   if (e != cudaSuccess) {
     ss_set_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
     delete c;
@@ -454,6 +478,7 @@ void ss_destroy(ss_ctx* c) {
   jobs_shutdown(c);
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->ana_stream) cudaStreamSynchronize(c->ana_stream);
   DevBuf* bufs[] = {&c->d_center, &c->d_npower, &c->d_nsto, &c->d_itype, &c->d_ng, &c->d_cg, &c->d_gg,
                     &c->d_gs, &c->d_pp, &c->d_ppf, &c->d_pp_off, &c->d_pp_cnt, &c->d_is, &c->d_js, &c->d_ks,
                     &c->d_ls, &c->d_precond, &c->d_gauss, &c->d_mean, &c->d_sigma, &c->d_scratch_a,
@@ -466,6 +491,14 @@ void ss_destroy(ss_ctx* c) {
     if (c->eri_join[s]) cudaEventDestroy(c->eri_join[s]);
   }
   if (c->eri_fork) cudaEventDestroy(c->eri_fork);
+  if (c->ana_stream) cudaStreamDestroy(c->ana_stream);
+  if (c->ana_fork) cudaEventDestroy(c->ana_fork);
+  if (c->ana_done) cudaEventDestroy(c->ana_done);
+  if (c->pin_evt) {
+    cudaEventSynchronize(c->pin_evt);
+    cudaEventDestroy(c->pin_evt);
+  }
+  if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -32,6 +32,15 @@ constexpr double PRIM_SCREEN_EPS = 1e-18;
 // this; every launch opts in to exactly this much, so concurrent launches from several host
 // threads (jobs) all set the same per-kernel attribute (a per-launch size would race).
 constexpr int ERI_SMEM_MAX = 60 * 1024;
+// Light-ket rule: the ket degree bound LK of the instance that evaluates a quartet whose pairs
+// have per-axis degree bounds L (the larger) and lmin (the smaller), the lighter pair taking the
+// ket; -1 for the full-L instance.  Instances exist for LK = lmin < L <= 3, and for L = 4 with
+// LK = max(lmin, 1) <= 2.
+__host__ __device__ inline int ss_light_ket(int L, int lmin) {
+  if (lmin >= L) return -1;
+  if (L == 4) return lmin <= 2 ? (lmin < 1 ? 1 : lmin) : -1;
+  return lmin;
+}
 // Where a quartet's partial sums (one per bra slice) live: slot code = offset << SLOT_SPLIT_BITS |
 // split, the partials being entries offset .. offset + split - 1 (split < 2^SLOT_SPLIT_BITS).
 constexpr int SLOT_SPLIT_BITS = 7;

@@ -54,6 +54,14 @@ struct ss_ctx {
   static constexpr int ERI_STREAMS = 4;
   cudaStream_t eri_stream[ERI_STREAMS] = {};
   cudaEvent_t eri_fork = nullptr, eri_join[ERI_STREAMS] = {};
+  // ss_two_e_job queues the analytic stage on ana_stream (ana_fork orders it after the context
+  // stream's earlier work, ana_done marks its end) while the MC runs on the context stream
+  cudaStream_t ana_stream = nullptr;
+  cudaEvent_t ana_fork = nullptr, ana_done = nullptr;
+  // pinned staging buffer of h2d_async (pin_evt: the last copy out of it)
+  void* pin = nullptr;
+  size_t pin_cap = 0;
+  cudaEvent_t pin_evt = nullptr;
   int64_t launches = 0;
   int num_sms = 0;
 
@@ -117,6 +125,9 @@ namespace ss {
 int dev_alloc(ss_ctx* c, DevBuf& b, size_t bytes);   // (re)allocates only when growing
 void dev_free(ss_ctx* c, DevBuf& b);
 int h2d(ss_ctx* c, DevBuf& b, const void* src, size_t bytes);
+// as h2d, through the context's pinned staging buffer, so that the call returns without waiting
+// for the stream (a pageable copy waits for the stream's earlier work)
+int h2d_async(ss_ctx* c, DevBuf& b, const void* src, size_t bytes);
 int ensure_precond(ss_ctx* c);
 // named pool buffer of at least `bytes`; *out receives the device pointer
 int pool_get(ss_ctx* c, const char* name, size_t bytes, void** out);

@@ -42,9 +42,8 @@ def _pair_L(b, f1, f2):
 def kernel_classes(b, quartets):
     """The analytic kernel instance (L, LK, tc) of every quartet, as the device buckets them:
     L = the larger pair's per-axis degree bound, tc = the number of r^2-type fits among the four
-    functions, LK = the lighter pair's bound (1 or 2) for L >= 3 quartets whose lighter pair has
-    L <= 2 and 1 for L = 2 quartets whose lighter pair has L <= 1, else L.  Returns an (nq, 3)
-    int array."""
+    functions, LK = the lighter pair's bound lmin for lmin < L <= 3, max(lmin, 1) for L = 4 and
+    lmin <= 2, else L.  Returns an (nq, 3) int array."""
     is_, js, ks, ls = [np.asarray(a) - 1 for a in quartets]
     n = b.n
     PL = np.zeros((n, n), dtype=np.int64)
@@ -56,8 +55,8 @@ def kernel_classes(b, quartets):
     lmin = np.minimum(Lb, Lk)
     r2 = (np.asarray(b.i_type) == 2).astype(np.int64)
     tc = r2[is_] + r2[ks] + r2[js] + r2[ls]
-    light = ((L >= 3) & (lmin <= 2)) | ((L == 2) & (lmin <= 1))
-    LK = np.where(light, np.maximum(lmin, 1), L)
+    # the light-ket rule of ss_light_ket (csrc/ss_common.cuh)
+    LK = np.where(lmin >= L, L, np.where(L == 4, np.where(lmin <= 2, np.maximum(lmin, 1), L), lmin))
     return np.stack([L, LK, tc], axis=1)
 
 

@@ -111,7 +111,13 @@ double quartet_value(const BasisDev& B, int fi, int fk, int fj, int fl, bool fol
 #define SS_HOST_DISPATCH(F, ...)                                   \
   do {                                                             \
     if (LK < L) {                                                  \
-      if (LK == 1) {                                               \
+      if (LK == 0) {                                               \
+        if (L == 1 && tc == 0) return F<1, 0, 0>(__VA_ARGS__);     \
+        if (L == 2 && tc == 0) return F<2, 0, 0>(__VA_ARGS__);     \
+        if (L == 2 && tc == 1) return F<2, 1, 0>(__VA_ARGS__);     \
+        if (L == 3 && tc == 0) return F<3, 0, 0>(__VA_ARGS__);     \
+        if (L == 3 && tc == 1) return F<3, 1, 0>(__VA_ARGS__);     \
+      } else if (LK == 1) {                                        \
         if (L == 2 && tc == 0) return F<2, 0, 1>(__VA_ARGS__);     \
         if (L == 2 && tc == 1) return F<2, 1, 1>(__VA_ARGS__);     \
         if (L == 3 && tc == 0) return F<3, 0, 1>(__VA_ARGS__);     \
@@ -298,13 +304,13 @@ int ss_host_eri(int n, int ld, const double* center, const int* npower, const in
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = (mode == 0 && ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1))) ? std::max(lmin, 1) : 0;
+    const int v = mode == 0 ? ss_light_ket(L, lmin) + 1 : 0;
     const bool swp = (v && Lk > Lb) || mode == 2;
     if (swp) {
       std::swap(i, j);
       std::swap(k, l);
     }
-    const int LK = v ? v : L;
+    const int LK = v ? v - 1 : L;
     lk_out[q] = LK;
     out[q] = dispatch(L, LK, tc, B, i, k, j, l, fold != 0, &bad);
   }
@@ -328,13 +334,13 @@ int ss_host_fp32_error(int n, int ld, const double* center, const int* npower, c
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1)) ? std::max(lmin, 1) : 0;
+    const int v = ss_light_ket(L, lmin) + 1;
     const double sch = std::sqrt(pre[i + (int64_t)n * k] * pre[j + (int64_t)n * l]);
     if (v && Lk > Lb) {
       std::swap(i, j);
       std::swap(k, l);
     }
-    if (dispatch_fp32(L, v ? v : L, tc, B, i, k, j, l, sch, eps32, &e)) return 1;
+    if (dispatch_fp32(L, v ? v - 1 : L, tc, B, i, k, j, l, sch, eps32, &e)) return 1;
   }
   out[0] = e.all;
   out[1] = e.tier;
@@ -386,9 +392,9 @@ int ss_host_tier_counts(int n, int ld, const double* center, const int* npower, 
     const int L = std::max(Lb, Lk);
     const int tc = (itype[i] == 2) + (itype[k] == 2) + (itype[j] == 2) + (itype[l] == 2);
     const int lmin = std::min(Lb, Lk);
-    const int v = ((L >= 3 && lmin <= 2) || (L == 2 && lmin <= 1)) ? std::max(lmin, 1) : 0;
+    const int v = ss_light_ket(L, lmin) + 1;
     cls[3 * q] = L;
-    cls[3 * q + 1] = v ? v : L;
+    cls[3 * q + 1] = v ? v - 1 : L;
     cls[3 * q + 2] = tc;
     const double sch = std::sqrt(pre[i + (int64_t)n * k] * pre[j + (int64_t)n * l]);
     const std::vector<double>& Sb = factors(i, k);

@@ -61,7 +61,7 @@ def test_host_kernel_matches_oracle_h2o26(lib, h2o26):
     got, lk = _host_eri(lib, b, q, mode=0)
     cls = perfmodel.kernel_classes(b, q)
     assert (cls[:, 1] == lk).all()  # the Python classifier picks the instances the host build uses
-    for L, LK in ((2, 1), (3, 1), (3, 2), (4, 1), (4, 2)):  # every light-ket bound is exercised
+    for L, LK in ((1, 0), (2, 0), (2, 1), (3, 0), (3, 1), (3, 2), (4, 1), (4, 2)):  # every light-ket bound is exercised
         assert ((cls[:, 0] == L) & (lk == LK)).sum() > 0, (L, LK)
     ok = _gate(got, ref, pre, q, b.n)
     assert ok.all(), f"{(~ok).sum()} quartets outside the gate"

@@ -73,3 +73,23 @@ def test_job_admission_limits():
         ctx.job_limits(eri_budget_bytes=foot // 2)
         with pytest.raises(SSError, match="budget"):
             ctx.job_submit(seed=6, **args)
+
+
+@pytest.mark.parametrize("estimator,precision", [("shared", "split_bf16"), ("faithful", "fp64")])
+def test_two_e_job_matches_staged_calls(estimator, precision):
+    """ss_two_e_job runs the analytic stage on its own stream beside the MC; the result is bitwise
+    that of the staged calls ss_gauss_eri, ss_zvmc and ss_combine on one stream, and the
+    context's later calls see the finished analytic stage."""
+    b = configs.h2o_26(ng0=6)
+    q = basis.build_mapping(b.n)
+    npts = 8000 if estimator == "faithful" else 1 << 16
+    with _ctx(b, q) as ctx:
+        e_job, s_job = ctx.two_e_job(1.8, 7, npts, 3, estimator, precision)
+        g_after, _ = ctx.gauss_eri()
+        ctx.invalidate()
+        g, _ = ctx.gauss_eri()
+        m, s = ctx.zvmc(1.8, 7, npts, 3, estimator, precision)
+        e = ctx.combine()
+    assert np.array_equal(g_after, g)
+    assert np.array_equal(e_job, e)
+    assert np.array_equal(s_job, s)
