@@ -113,12 +113,20 @@ def test_gauss_eri_h2o26_ng20_stratified(h2o26_ng20, fp32_eps):
     P = pre.reshape(n, n, order="F")
     i, j, k, l = [a - 1 for a in sub]
     bound = RTOL * np.abs(ref) + RTOL * np.sqrt(np.abs(P[i, k] * P[j, l]))
-    ratio = np.abs(g[sel] - ref) / bound
+    ratio = _gate_ratio(np.abs(g[sel] - ref), bound)
     worst = int(np.argmax(ratio))
     print(f"\nh2o_26 ng0=20 fp32_eps={fp32_eps:g}: {sel.size} quartets vs oracle, worst |gpu-oracle|/gate "
           f"{ratio[worst]:.3e} (quartet {[int(x[worst]) for x in sub]}, FP32 share {share[sel][worst]:.2f}); "
           f"largest FP32 share in the sample {share[sel].max():.3f}")
     assert np.all(ratio <= 1.0), f"{(ratio > 1).sum()} quartets outside the gate, worst ratio {ratio.max():.3g}"
+
+
+def _gate_ratio(diff, bound):
+    """|gpu - oracle| / gate per quartet; a quartet with a zero gate (a pair whose Schwarz
+    diagonal is exactly zero, e.g. two distant functions whose primitive pairs all vanish) must
+    match exactly (ratio 0, else inf)."""
+    safe = np.where(bound > 0, bound, 1.0)
+    return np.where(bound > 0, diff / safe, np.where(diff == 0, 0.0, np.inf))
 
 
 def test_gauss_eri_golden_ng20():
@@ -170,7 +178,7 @@ def test_gauss_eri_random_molecule_subset():
     ref, _ = O.gauss_eri(ob, sub, pre.reshape(-1, order="F"))
     i, j, k, l = [a - 1 for a in sub]
     bound = RTOL * np.abs(ref) + RTOL * np.sqrt(np.abs(pre[i, k] * pre[j, l]))
-    ratio = np.abs(g - ref) / bound
+    ratio = _gate_ratio(np.abs(g - ref), bound)
     print(f"\nrandom molecule (111 STOs): {sel.size} quartets of {len(keys)} vs oracle, "
           f"{len(np.unique(keys))} kernel instances, worst |gpu-oracle|/gate {ratio.max():.3e}")
     assert np.all(ratio <= 1.0), f"{(ratio > 1).sum()} quartets outside the gate, worst {ratio.max():.3g}"
