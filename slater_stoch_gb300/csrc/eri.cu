@@ -172,6 +172,8 @@ void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem) {
   // SM (8 warps) and leave unified L1 to the local arrays of the classes with r^2-type fits.  On
   // the 26-function H2O basis 168 KB (one CTA per SM) -> 60 KB tiles took the analytic stage from
   // 2.71 to 2.53 s.
+  // (smaller tiles for the spilling LK = L >= 3 instances, to leave L1 to their local arrays,
+  // were slower: 32 KB -> 1.458 s, 16 KB -> 1.473 s for the analytic stage, against 1.446 s)
   const size_t budget = (size_t)ERI_SMEM_MAX;
   int kt = (int)(budget / per);
   kt = kt < max_cnt ? kt : max_cnt;

@@ -52,11 +52,29 @@ __device__ __forceinline__ float mixture_density(const MixDev& M, int d, const f
   return tot;
 }
 
-// Samples of one block: u1, u2 [3S] (double), w [S].  Per sample one Philox4x32-10 call for
-// each electron: word 0 picks the mixture component (equal weights: floor(word * m / 2^32)),
-// words 1..3 give r ~ N(0, I3); the ZV map u = G_c + c |r| r (offset in FP32).
-__global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, MixDev M, double* __restrict__ u1,
-                                     double* __restrict__ u2, double* __restrict__ w) {
+// Samples of one block.  Per sample one Philox4x32-10 call for each electron: word 0 picks the
+// mixture component (equal weights: floor(word * m / 2^32)), words 1..3 give r ~ N(0, I3); the ZV
+// map u = G_c + c |r| r (offset in FP32).  Output: SampleF64 (u1, u2 [3S] double, w [S] double;
+// ss_shared_samples) or SampleF32 (u as two-float hi + lo [3S] each, w [S] float; the estimator's
+// own kernels, which then run without FP64 instructions).
+struct SampleF64 {
+  static constexpr bool f64 = true;
+  double *u1, *u2, *w;
+};
+struct SampleF32 {
+  static constexpr bool f64 = false;
+  float *u1h, *u1l, *u2h, *u2l, *w;
+};
+
+// hi + lo = a + b (Knuth's two-sum, exact in round-to-nearest)
+__device__ __forceinline__ void two_sum(float a, float b, float& hi, float& lo) {
+  hi = a + b;
+  const float bb = hi - a;
+  lo = (a - (hi - bb)) + (b - bb);
+}
+
+template <class Out>
+__global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, MixDev M, Out out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= S) return;
   const int64_t g = first + s;
@@ -80,11 +98,22 @@ __global__ void shared_sample_kernel(uint64_t seed, int64_t first, int64_t S, Mi
     const float dl = (M.Gf[3 * d[0] + l] - M.Gf[3 * d[1] + l]) +
                      ((M.Glo[3 * d[0] + l] - M.Glo[3 * d[1] + l]) + (off[0][l] - off[1][l]));
     r2 = fmaf(dl, dl, r2);
-    u1[3 * s + l] = M.G[3 * d[0] + l] + (double)off[0][l];
-    u2[3 * s + l] = M.G[3 * d[1] + l] + (double)off[1][l];
+    if constexpr (Out::f64) {
+      out.u1[3 * s + l] = M.G[3 * d[0] + l] + (double)off[0][l];
+      out.u2[3 * s + l] = M.G[3 * d[1] + l] + (double)off[1][l];
+    } else {  // u = Gf + Glo + off to ~2^-48 relative
+      float h, lo;
+      two_sum(M.Gf[3 * d[0] + l], off[0][l], h, lo);
+      out.u1h[3 * s + l] = h;
+      out.u1l[3 * s + l] = lo + M.Glo[3 * d[0] + l];
+      two_sum(M.Gf[3 * d[1] + l], off[1][l], h, lo);
+      out.u2h[3 * s + l] = h;
+      out.u2l[3 * s + l] = lo + M.Glo[3 * d[1] + l];
+    }
   }
   const float ww = 1.0f / (sqrtf(r2) * p1 * p2);
-  w[s] = isfinite(ww) ? (double)ww : 0.0;
+  if constexpr (Out::f64) out.w[s] = isfinite(ww) ? (double)ww : 0.0;
+  else out.w[s] = isfinite(ww) ? ww : 0.f;
 }
 
 // Fit residual of one shell as a function of t = sqrt(r): cubic Hermite table on a uniform grid
@@ -105,14 +134,16 @@ struct ResidDev {
 // residual), so the whole evaluation runs in FP32: u_orb = r^n_sto e^(-zeta r), u_gauss = u_orb -
 // delta.  One block row per shell (consecutive functions sharing centre, STO exponent and fit,
 // which differ only by their cartesian monomial).  out[plane][i][s], planes {S1,G1,D1,S2,G2,D2}.
+// Coordinates relative to the shell centre from two-float samples and centres:
+// (uh - Ah) + (ul - Al), exact in its first difference wherever u is near A.
 __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, const int* __restrict__ shell_start,
-                                         ResidDev R, const double* __restrict__ u1,
-                                         const double* __restrict__ u2, float* __restrict__ out) {
+                                         ResidDev R, const float* __restrict__ Ahl, SampleF32 U,
+                                         float* __restrict__ out) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int sh = blockIdx.y;
   if (s >= S) return;
   const int i = shell_start[sh], i_end = shell_start[sh + 1];
-  const double* A = B.center + 3 * i;
+  const float* Ah = Ahl + 6 * sh;  // centre hi[3], lo[3]
   const int nsto = B.n_sto[i];
   const float zeta = (float)B.g_slater[i];
   const float2* tab = R.node + R.off[sh];
@@ -121,8 +152,11 @@ __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, cons
   const int64_t plane = (int64_t)B.n * ld;
 #pragma unroll
   for (int e = 0; e < 2; e++) {
-    const double* u = e == 0 ? u1 : u2;
-    const float dx = (float)(u[3 * s] - A[0]), dy = (float)(u[3 * s + 1] - A[1]), dz = (float)(u[3 * s + 2] - A[2]);
+    const float* uh = e == 0 ? U.u1h : U.u2h;
+    const float* ul = e == 0 ? U.u1l : U.u2l;
+    const float dx = (uh[3 * s] - Ah[0]) + (ul[3 * s] - Ah[3]);
+    const float dy = (uh[3 * s + 1] - Ah[1]) + (ul[3 * s + 1] - Ah[4]);
+    const float dz = (uh[3 * s + 2] - Ah[2]) + (ul[3 * s + 2] - Ah[5]);
     const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
     float uo = expf(-zeta * r);
     for (int t = 0; t < nsto; t++) uo *= r;
@@ -160,7 +194,7 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 // K = 2*Kh (Kh >= S, padded samples are zero); hi/lo BF16 split.
 __global__ void shared_operand_kernel(int64_t S, int64_t Kh, int64_t ld, int n, const int* __restrict__ pi,
                                       const int* __restrict__ pk, const float* __restrict__ F,
-                                      const double* __restrict__ w, __nv_bfloat16* __restrict__ Ahi,
+                                      const float* __restrict__ w, __nv_bfloat16* __restrict__ Ahi,
                                       __nv_bfloat16* __restrict__ Alo, __nv_bfloat16* __restrict__ Bhi,
                                       __nv_bfloat16* __restrict__ Blo) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -177,7 +211,7 @@ __global__ void shared_operand_kernel(int64_t S, int64_t Kh, int64_t ld, int n, 
     const float* F2G = F + 4 * plane;
     const float* F2D = F + 5 * plane;
     const int64_t oi = (int64_t)i * ld + s, ok = (int64_t)k * ld + s;
-    const float ww = (float)w[s];
+    const float ww = w[s];
     // rhoS - rhoG = phiS_i delta_k + delta_i phiG_k (exact identity, no cancellation)
     d1 = fmaf(F1S[oi], F1D[ok], F1D[oi] * F1G[ok]);
     g1 = F1G[oi] * F1G[ok];
@@ -193,14 +227,23 @@ __global__ void shared_operand_kernel(int64_t S, int64_t Kh, int64_t ld, int n, 
   split_bf16(d2w, h, l); Bhi[r + Kh + s] = h; Blo[r + Kh + s] = l;
 }
 
-// Cblk[P][P] (double) += sum over K slices of the fp32 partial products
+// Cblk[P][P] (double) += sum over K slices of the fp32 partial products.  The slices are summed
+// as an unevaluated FP32 pair hi + lo (two-sum: hi exact-rounded, lo collecting the rounding
+// errors; error ~2^-48 of the sum of magnitudes, as a double sum of the FP32 partials) so that
+// the FP64 pipe sees two conversions and two adds per element instead of 2 per slice.
 __global__ void shared_accumulate_block(int P, int ksplit, const float* __restrict__ Cp, double* __restrict__ Cblk) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t PP = (int64_t)P * P;
   if (e >= PP) return;
-  double v = 0.0;
-  for (int t = 0; t < ksplit; t++) v += (double)Cp[t * PP + e];
-  Cblk[e] += v;
+  float hi = 0.f, lo = 0.f;
+#pragma unroll 4
+  for (int t = 0; t < ksplit; t++) {
+    float h, l;
+    two_sum(hi, Cp[t * PP + e], h, l);
+    hi = h;
+    lo += l;
+  }
+  Cblk[e] += (double)hi + (double)lo;
 }
 
 // per-quartet block value x = (C[ik][jl] + C[jl][ik]) / (2 npts)  (electron-swap symmetrised)
@@ -239,6 +282,7 @@ struct SharedPlan {
   int* d_pi = nullptr; int* d_pk = nullptr; int* d_p1 = nullptr; int* d_p2 = nullptr;
   std::vector<int> shell_start;     // consecutive functions with identical radial part
   int* d_shell = nullptr;
+  float* d_Ahl = nullptr;           // per shell: centre as float hi[3], lo[3]
   MixDev mix{};
   ResidDev resid{};
 };
@@ -416,6 +460,15 @@ static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
     if (!same_radial(c, f, S.shell_start.back())) S.shell_start.push_back(f);
   S.shell_start.push_back(c->n);
   TRY(upload_v(c, "sh_shell", S.shell_start, &S.d_shell));
+  std::vector<float> Ahl(6 * (S.shell_start.size() - 1));
+  for (size_t sh = 0; sh + 1 < S.shell_start.size(); sh++)
+    for (int l = 0; l < 3; l++) {
+      const double A = c->h_center[3 * (size_t)S.shell_start[sh] + l];
+      const float hi = (float)A;
+      Ahl[6 * sh + l] = hi;
+      Ahl[6 * sh + 3 + l] = (float)(A - (double)hi);
+    }
+  TRY(upload_v(c, "sh_Ahl", Ahl, &S.d_Ahl));
   TRY(build_resid_tables(c, S.shell_start, &S.resid));
   return SS_OK;
 }
@@ -429,8 +482,14 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
   TRY(build_shared_plan(c, a_zv, SP));
   const int P = SP.npairs, n = c->n;
   const int64_t nint = c->nint;
-  // sub-chunk of samples whose GEMM accumulates in one FP32 TMEM accumulator
-  const int64_t Sc = std::min<int64_t>(npts, 65536);
+  // sub-chunk of samples whose GEMM accumulates in one FP32 TMEM accumulator: up to 262,144
+  // samples while its BF16 operands (16 P bytes per sample) stay within 1.5 GB, at least 65,536.
+  // Fewer, longer sub-chunks amortise the per-sub-chunk launches, K-slice epilogues and partial
+  // sums (26-function H2O job, 2^26 pairs: 65,536 -> 262,144 samples took the job from 1.695
+  // to 1.654 s; smaller sub-chunks whose operands would stay in L2 were slower: 16,384 -> 1.96 s).
+  int64_t sc_max = 262144;
+  while (sc_max > 65536 && 16.0 * P * (double)sc_max > 1.5e9) sc_max /= 2;
+  const int64_t Sc = std::min<int64_t>(npts, sc_max);
   const int64_t Kh = (Sc + 31) / 32 * 32;  // K = 2 Kh is a multiple of 64
   const int64_t K = 2 * Kh;
   const int T = (P + 127) / 128;
@@ -439,13 +498,17 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
   // nearly empty wave costs as much as a full one (GEMM 113.5 -> 103.1 ms per job)
   int ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(ktiles, (2 * c->num_sms) / (T * T)));
   void* p;
-  double *u1, *u2, *w, *Cblk, *acc, *acc2;
-  float *F, *Cp;
+  double *Cblk, *acc, *acc2;
+  float *F, *Cp, *w;
+  SampleF32 smp;
   __nv_bfloat16 *Ahi, *Alo, *Bhi, *Blo;
   int* err;
-  TRY(pool_get(c, "sh_u1", sizeof(double) * 3 * Sc, &p)); u1 = (double*)p;
-  TRY(pool_get(c, "sh_u2", sizeof(double) * 3 * Sc, &p)); u2 = (double*)p;
-  TRY(pool_get(c, "sh_w", sizeof(double) * Sc, &p)); w = (double*)p;
+  TRY(pool_get(c, "sh_u1h", sizeof(float) * 3 * Sc, &p)); smp.u1h = (float*)p;
+  TRY(pool_get(c, "sh_u1l", sizeof(float) * 3 * Sc, &p)); smp.u1l = (float*)p;
+  TRY(pool_get(c, "sh_u2h", sizeof(float) * 3 * Sc, &p)); smp.u2h = (float*)p;
+  TRY(pool_get(c, "sh_u2l", sizeof(float) * 3 * Sc, &p)); smp.u2l = (float*)p;
+  TRY(pool_get(c, "sh_w", sizeof(float) * Sc, &p)); w = (float*)p;
+  smp.w = w;
   TRY(pool_get(c, "sh_F", sizeof(float) * 6 * (size_t)n * Sc, &p)); F = (float*)p;
   const size_t opb = sizeof(__nv_bfloat16) * (size_t)P * K;
   TRY(pool_get(c, "sh_Ahi", opb, &p)); Ahi = (__nv_bfloat16*)p;
@@ -471,10 +534,10 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
     for (int64_t c0 = 0; c0 < npts; c0 += Sc) {
       const int64_t ns = std::min(Sc, npts - c0);
       const int64_t first = (int64_t)b * npts + c0;
-      shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, u1, u2, w);
+      shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, smp);
       SS_CUDA_TRY(cudaGetLastError());
       shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)(SP.shell_start.size() - 1)), 128, 0,
-                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, SP.resid, u1, u2, F);
+                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, SP.resid, SP.d_Ahl, smp, F);
       SS_CUDA_TRY(cudaGetLastError());
       shared_operand_kernel<<<dim3((unsigned)((Kh + 255) / 256), (unsigned)P), 256, 0, c->stream>>>(
           ns, Kh, Sc, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);
@@ -597,8 +660,8 @@ extern "C" int ss_shared_samples(ss_ctx* c, double a_zv, uint64_t seed, int64_t 
   TRY(pool_get(c, "smp_u1", sizeof(double) * 3 * S, &a));
   TRY(pool_get(c, "smp_u2", sizeof(double) * 3 * S, &b));
   TRY(pool_get(c, "smp_w", sizeof(double) * S, &ww));
-  shared_sample_kernel<<<(unsigned)((S + 127) / 128), 128, 0, c->stream>>>(seed, first, S, SP.mix, (double*)a,
-                                                                          (double*)b, (double*)ww);
+  shared_sample_kernel<<<(unsigned)((S + 127) / 128), 128, 0, c->stream>>>(
+      seed, first, S, SP.mix, SampleF64{(double*)a, (double*)b, (double*)ww});
   SS_CUDA_TRY(cudaGetLastError());
   c->launches++;
   SS_CUDA_TRY(cudaMemcpyAsync(u1, a, sizeof(double) * 3 * S, cudaMemcpyDeviceToHost, c->stream));

@@ -23,13 +23,13 @@ EXEC_FLOPS_PER_PRIM = 241.5
 # workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job, at
 # the default tiers (primitive screen 1e-18, FP32 tier below 1e-11 of the Schwarz bound)
 EXEC_FLOPS = {
-    "h2o_26_ng20": (6.003e11, 4.777e11),
+    "h2o_26_ng20": (5.878e11, 4.787e11),
 }
 # workload -> DRAM bytes (read + write) of all eri_kernel launches of one job (ncu
 # dram__bytes_read.sum + dram__bytes_write.sum, one pass each; mostly the local-memory spill
 # traffic of the L = 4 classes with several r^2-type fits)
 EXEC_DRAM_BYTES = {
-    "h2o_26_ng20": 1.157e10,
+    "h2o_26_ng20": 1.157e10,  # 1.1570e10 (with the LK = 0, 1 light-ket instances of L <= 3)
 }
 
 
