@@ -143,9 +143,9 @@ __global__ void shared_fn_density_kernel(BasisDev B, int64_t S, int64_t ld, cons
   const int sh = blockIdx.y;
   if (s >= S) return;
   const int i = shell_start[sh], i_end = shell_start[sh + 1];
-  const float* Ah = Ahl + 6 * sh;  // centre hi[3], lo[3]
+  const float* Ah = Ahl + 8 * sh;  // centre hi[3], lo[3], STO exponent, pad
   const int nsto = B.n_sto[i];
-  const float zeta = (float)B.g_slater[i];
+  const float zeta = Ah[6];
   const float2* tab = R.node + R.off[sh];
   const int nint = R.off[sh + 1] - R.off[sh] - 1;
   const float inv_h = R.inv_h[sh], tmax = R.tmax[sh];
@@ -191,40 +191,109 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 }
 
 // operands of one sub-chunk: A = [Delta1 | rhoG1], B = [rhoS2 w | Delta2 w], rows = pairs,
-// K = 2*Kh (Kh >= S, padded samples are zero); hi/lo BF16 split.
+// K = 2*Kh (Kh >= S, padded samples are zero); hi/lo BF16 split.  Each thread forms V consecutive
+// samples of one pair (vector loads of the orbital values, V*2-byte stores of each operand
+// plane); ld (the orbital-value row stride) and Kh are multiples of V.
+template <int V>
+struct VecF;
+template <>
+struct VecF<1> {
+  static __device__ __forceinline__ void load(const float* p, float (&x)[1]) { x[0] = *p; }
+};
+template <>
+struct VecF<2> {
+  static __device__ __forceinline__ void load(const float* p, float (&x)[2]) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    x[0] = v.x; x[1] = v.y;
+  }
+};
+template <>
+struct VecF<4> {
+  static __device__ __forceinline__ void load(const float* p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+  }
+};
+template <>
+struct VecF<8> {
+  static __device__ __forceinline__ void load(const float* p, float (&x)[8]) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+  }
+};
+
+// V bf16 values as one V*2-byte store
+template <int V>
+__device__ __forceinline__ void store_bf16(__nv_bfloat16* dst, const __nv_bfloat16 (&v)[V]) {
+  if constexpr (V == 1) {
+    dst[0] = v[0];
+  } else {
+    uint32_t w32[V / 2];
+#pragma unroll
+    for (int t = 0; t < V / 2; t++)
+      w32[t] = (uint32_t)__bfloat16_as_ushort(v[2 * t]) | ((uint32_t)__bfloat16_as_ushort(v[2 * t + 1]) << 16);
+    if constexpr (V == 2) *reinterpret_cast<uint32_t*>(dst) = w32[0];
+    else if constexpr (V == 4) *reinterpret_cast<uint2*>(dst) = make_uint2(w32[0], w32[1]);
+    else *reinterpret_cast<uint4*>(dst) = make_uint4(w32[0], w32[1], w32[2], w32[3]);
+  }
+}
+
+template <int V>
 __global__ void shared_operand_kernel(int64_t S, int64_t Kh, int64_t ld, int n, const int* __restrict__ pi,
                                       const int* __restrict__ pk, const float* __restrict__ F,
                                       const float* __restrict__ w, __nv_bfloat16* __restrict__ Ahi,
                                       __nv_bfloat16* __restrict__ Alo, __nv_bfloat16* __restrict__ Bhi,
                                       __nv_bfloat16* __restrict__ Blo) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int p = blockIdx.y;
-  if (s >= Kh) return;
-  float d1 = 0.f, g1 = 0.f, s2w = 0.f, d2w = 0.f;
-  if (s < S) {
+  // pairs along x: consecutive CTAs read the orbital values of the same samples, which stay in
+  // L2 while all pairs use them (with samples along x the whole sub-chunk's values, 24 n bytes
+  // per sample, streamed through L2 once per pair)
+  const int64_t s0 = (blockIdx.y * (int64_t)blockDim.x + threadIdx.x) * V;
+  const int p = blockIdx.x;
+  if (s0 >= Kh) return;
+  float d1[V], g1[V], s2w[V], d2w[V];
+#pragma unroll
+  for (int e = 0; e < V; e++) d1[e] = g1[e] = s2w[e] = d2w[e] = 0.f;
+  if (s0 < S) {
     const int i = pi[p], k = pk[p];
     const int64_t plane = (int64_t)n * ld;
-    const float* F1S = F;
-    const float* F1G = F + plane;
-    const float* F1D = F + 2 * plane;
-    const float* F2S = F + 3 * plane;
-    const float* F2G = F + 4 * plane;
-    const float* F2D = F + 5 * plane;
-    const int64_t oi = (int64_t)i * ld + s, ok = (int64_t)k * ld + s;
-    const float ww = w[s];
-    // rhoS - rhoG = phiS_i delta_k + delta_i phiG_k (exact identity, no cancellation)
-    d1 = fmaf(F1S[oi], F1D[ok], F1D[oi] * F1G[ok]);
-    g1 = F1G[oi] * F1G[ok];
-    s2w = (F2S[oi] * F2S[ok]) * ww;
-    d2w = fmaf(F2S[oi], F2D[ok], F2D[oi] * F2G[ok]) * ww;
+    const int64_t oi = (int64_t)i * ld + s0, ok = (int64_t)k * ld + s0;
+    float a1S[V], a1G[V], a1D[V], b1G[V], b1D[V], a2S[V], a2D[V], b2S[V], b2G[V], b2D[V], ww[V];
+    VecF<V>::load(F + oi, a1S);
+    VecF<V>::load(F + plane + oi, a1G);
+    VecF<V>::load(F + 2 * plane + oi, a1D);
+    VecF<V>::load(F + plane + ok, b1G);
+    VecF<V>::load(F + 2 * plane + ok, b1D);
+    VecF<V>::load(F + 3 * plane + oi, a2S);
+    VecF<V>::load(F + 5 * plane + oi, a2D);
+    VecF<V>::load(F + 3 * plane + ok, b2S);
+    VecF<V>::load(F + 4 * plane + ok, b2G);
+    VecF<V>::load(F + 5 * plane + ok, b2D);
+    VecF<V>::load(w + s0, ww);
+#pragma unroll
+    for (int e = 0; e < V; e++) {
+      if (s0 + e >= S) break;  // samples past the sub-chunk's end stay zero
+      // rhoS - rhoG = phiS_i delta_k + delta_i phiG_k (exact identity, no cancellation)
+      d1[e] = fmaf(a1S[e], b1D[e], a1D[e] * b1G[e]);
+      g1[e] = a1G[e] * b1G[e];
+      s2w[e] = (a2S[e] * b2S[e]) * ww[e];
+      d2w[e] = fmaf(a2S[e], b2D[e], a2D[e] * b2G[e]) * ww[e];
+    }
   }
   const int64_t K = 2 * Kh;
-  const int64_t r = (int64_t)p * K;
-  __nv_bfloat16 h, l;
-  split_bf16(d1, h, l); Ahi[r + s] = h; Alo[r + s] = l;
-  split_bf16(g1, h, l); Ahi[r + Kh + s] = h; Alo[r + Kh + s] = l;
-  split_bf16(s2w, h, l); Bhi[r + s] = h; Blo[r + s] = l;
-  split_bf16(d2w, h, l); Bhi[r + Kh + s] = h; Blo[r + Kh + s] = l;
+  const int64_t r = (int64_t)p * K + s0;
+  __nv_bfloat16 h[V], l[V];
+#pragma unroll
+  for (int e = 0; e < V; e++) split_bf16(d1[e], h[e], l[e]);
+  store_bf16<V>(Ahi + r, h); store_bf16<V>(Alo + r, l);
+#pragma unroll
+  for (int e = 0; e < V; e++) split_bf16(g1[e], h[e], l[e]);
+  store_bf16<V>(Ahi + r + Kh, h); store_bf16<V>(Alo + r + Kh, l);
+#pragma unroll
+  for (int e = 0; e < V; e++) split_bf16(s2w[e], h[e], l[e]);
+  store_bf16<V>(Bhi + r, h); store_bf16<V>(Blo + r, l);
+#pragma unroll
+  for (int e = 0; e < V; e++) split_bf16(d2w[e], h[e], l[e]);
+  store_bf16<V>(Bhi + r + Kh, h); store_bf16<V>(Blo + r + Kh, l);
 }
 
 // Cblk[P][P] (double) += sum over K slices of the fp32 partial products.  The slices are summed
@@ -282,7 +351,7 @@ struct SharedPlan {
   int* d_pi = nullptr; int* d_pk = nullptr; int* d_p1 = nullptr; int* d_p2 = nullptr;
   std::vector<int> shell_start;     // consecutive functions with identical radial part
   int* d_shell = nullptr;
-  float* d_Ahl = nullptr;           // per shell: centre as float hi[3], lo[3]
+  float* d_Ahl = nullptr;           // per shell: centre as float hi[3], lo[3], STO exponent, pad
   MixDev mix{};
   ResidDev resid{};
 };
@@ -460,14 +529,16 @@ static int build_shared_plan(ss_ctx* c, double a_zv, SharedPlan& S) {
     if (!same_radial(c, f, S.shell_start.back())) S.shell_start.push_back(f);
   S.shell_start.push_back(c->n);
   TRY(upload_v(c, "sh_shell", S.shell_start, &S.d_shell));
-  std::vector<float> Ahl(6 * (S.shell_start.size() - 1));
-  for (size_t sh = 0; sh + 1 < S.shell_start.size(); sh++)
+  std::vector<float> Ahl(8 * (S.shell_start.size() - 1), 0.f);
+  for (size_t sh = 0; sh + 1 < S.shell_start.size(); sh++) {
     for (int l = 0; l < 3; l++) {
       const double A = c->h_center[3 * (size_t)S.shell_start[sh] + l];
       const float hi = (float)A;
-      Ahl[6 * sh + l] = hi;
-      Ahl[6 * sh + 3 + l] = (float)(A - (double)hi);
+      Ahl[8 * sh + l] = hi;
+      Ahl[8 * sh + 3 + l] = (float)(A - (double)hi);
     }
+    Ahl[8 * sh + 6] = (float)c->h_gs[S.shell_start[sh]];
+  }
   TRY(upload_v(c, "sh_Ahl", Ahl, &S.d_Ahl));
   TRY(build_resid_tables(c, S.shell_start, &S.resid));
   return SS_OK;
@@ -507,9 +578,12 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
   TRY(pool_get(c, "sh_u1l", sizeof(float) * 3 * Sc, &p)); smp.u1l = (float*)p;
   TRY(pool_get(c, "sh_u2h", sizeof(float) * 3 * Sc, &p)); smp.u2h = (float*)p;
   TRY(pool_get(c, "sh_u2l", sizeof(float) * 3 * Sc, &p)); smp.u2l = (float*)p;
-  TRY(pool_get(c, "sh_w", sizeof(float) * Sc, &p)); w = (float*)p;
+  // orbital-value rows and weights padded to a multiple of 8 samples (the operand kernel's vector
+  // loads); entries past a sub-chunk's last sample are never used
+  const int64_t ldF = (Sc + 7) / 8 * 8;
+  TRY(pool_get(c, "sh_w", sizeof(float) * ldF, &p)); w = (float*)p;
   smp.w = w;
-  TRY(pool_get(c, "sh_F", sizeof(float) * 6 * (size_t)n * Sc, &p)); F = (float*)p;
+  TRY(pool_get(c, "sh_F", sizeof(float) * 6 * (size_t)n * ldF, &p)); F = (float*)p;
   const size_t opb = sizeof(__nv_bfloat16) * (size_t)P * K;
   TRY(pool_get(c, "sh_Ahi", opb, &p)); Ahi = (__nv_bfloat16*)p;
   TRY(pool_get(c, "sh_Alo", opb, &p)); Alo = (__nv_bfloat16*)p;
@@ -537,10 +611,12 @@ int run_shared(ss_ctx* c, double a_zv, uint64_t seed, int64_t npts, int nblocks,
       shared_sample_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, c->stream>>>(seed, first, ns, SP.mix, smp);
       SS_CUDA_TRY(cudaGetLastError());
       shared_fn_density_kernel<<<dim3((unsigned)((ns + 127) / 128), (unsigned)(SP.shell_start.size() - 1)), 128, 0,
-                                 c->stream>>>(c->basis, ns, Sc, SP.d_shell, SP.resid, SP.d_Ahl, smp, F);
+                                 c->stream>>>(c->basis, ns, ldF, SP.d_shell, SP.resid, SP.d_Ahl, smp, F);
       SS_CUDA_TRY(cudaGetLastError());
-      shared_operand_kernel<<<dim3((unsigned)((Kh + 255) / 256), (unsigned)P), 256, 0, c->stream>>>(
-          ns, Kh, Sc, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);
+      // four samples per thread (8-byte stores): per job 0.263 s of MC with one, 0.245 s with
+      // two, 0.226 s with four, 0.262 s with eight
+      shared_operand_kernel<4><<<dim3((unsigned)P, (unsigned)((Kh / 4 + 255) / 256)), 256, 0, c->stream>>>(
+          ns, Kh, ldF, n, SP.d_pi, SP.d_pk, F, w, Ahi, Alo, Bhi, Blo);
       SS_CUDA_TRY(cudaGetLastError());
       TRY(launch_split_bf16_gemm(c->stream, Ahi, Alo, Bhi, Blo, P, K, ksplit, Cp, err));
       shared_accumulate_block<<<(unsigned)((PP + 255) / 256), 256, 0, c->stream>>>(P, ksplit, Cp, Cblk);
