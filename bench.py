@@ -484,6 +484,29 @@ def main():
                           f"of the FP32 tier; {nprim:.4g} primitive quartets before screening")
                 if wl in EXEC_FLOPS else f"{nprim:.4g} primitive quartets x FP64 flops per primitive quartet"}
 
+    # the MC stage: HBM-bound.  Algorithmic bytes 32 P S per job (the BF16 hi/lo operands of both
+    # sides written once and read once by the tcgen05 GEMM); traffic = the DRAM bytes per sample
+    # of the MC kernels from their ncu capture, times the walker pairs
+    from slater_stoch_gb300.perfmodel import MC_DRAM_BYTES_PER_SAMPLE
+    npair = b.n * (b.n + 1) // 2
+    mc_alg = 32.0 * npair * args.walkers
+    hbm_peak, hbm_src = 6800.0, "fallback (no MEASURED_PEAKS.json)"
+    try:
+        hbm_peak = float(json.load(open(Path(__file__).resolve().parent / "MEASURED_PEAKS.json"))["hbm_gbs"])
+        hbm_src = "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except (OSError, KeyError, ValueError):
+        pass
+    mc_ach = mc_alg / t_mc / 1e9
+    mc_roofline = {"bound": "hbm", "achieved": mc_ach, "peak": hbm_peak, "unit": "GB/s", "frac": mc_ach / hbm_peak,
+                   "peak_source": hbm_src,
+                   "traffic": MC_DRAM_BYTES_PER_SAMPLE.get(wl, 0.0) * args.walkers or None,
+                   "traffic_note": "DRAM bytes of the MC kernels of one job (ncu capture of one sub-chunk, "
+                                   "scaled by the walker pairs)",
+                   "kernel": "shared-walker MC stage (sampler, orbital values, operands, tcgen05 GEMM, "
+                             "accumulation), timed alone",
+                   "units": f"algorithmic bytes 32 P S = {mc_alg:.4g} (P = {npair} function pairs, "
+                            f"S = {args.walkers} walker pairs)"}
+
     if rank == 0:
         lat = sorted(times)
         line = {
@@ -505,7 +528,7 @@ def main():
             "e2e": {"value": whole_job_throughput(nint, world, e2e_s), "unit": "ERIs/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "roofline": roofline,
+            "roofline": roofline, "mc_roofline": mc_roofline,
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
         }

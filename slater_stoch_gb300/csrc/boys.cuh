@@ -123,8 +123,11 @@ SS_HD void boys_tab(double T, int nf, double (&F)[NF + 1], const double* tab) {
   const double* lo = tab + BOYS_HI_K * BOYS_HI_J;
   const double* e2 = lo + BOYS_LO_K * BOYS_LO_N;
   const double sqpi = 1.7724538509055160273;  // dsqrt(dacos(-1.d0))
-  if (T < 1.0) {
-    if (T == 0.0) {
+  // T >= 0: its range tests compare the bit pattern on the integer pipe (for non-negative
+  // doubles the patterns order as the values), leaving the FP64 pipe to the arithmetic
+  const int64_t tb = bits_of(T);
+  if (tb < 0x3FF0000000000000LL) {  // T < 1
+    if (tb == 0) {                   // T == +0
 #pragma unroll
       for (int n = 0; n <= NF; n++) F[n] = 1.0 / (2 * n + 1);
       return;
@@ -138,10 +141,10 @@ SS_HD void boys_tab(double T, int nf, double (&F)[NF + 1], const double* tab) {
       else if (n < nf) F[n] = fma(T + T, F[n + 1 <= NF ? n + 1 : NF], e) * (1.0 / (2 * n + 1));
     }
   } else {
-    const double v = (T > 80.0) ? 0.0 : exp_neg(-T, e2);
+    const double v = (tb > 0x4054000000000000LL) ? 0.0 : exp_neg(-T, e2);  // T > 80
     const double u_inv = rsqrt_d(T);
     const double two_rho_inv = 0.5 * u_inv * u_inv;
-    const double val0 = (T > 36.0) ? 0.5 * u_inv * sqpi : boys0_hi(T, hi);
+    const double val0 = (tb > 0x4042000000000000LL) ? 0.5 * u_inv * sqpi : boys0_hi(T, hi);  // T > 36
     F[0] = val0;
     double rt = (val0 - v) * two_rho_inv;
     double di = 3.0;

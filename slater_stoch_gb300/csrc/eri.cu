@@ -130,7 +130,7 @@ __global__ void prim_pair_fill(BasisDev B, int npairs, const int64_t* __restrict
       if (fold && m1 != m2) r.coef = 2.0 * r.coef;
       r.pad[0] = 0.0;                    // Schwarz factor, set by the ERI kernel's self mode
       r.pad[1] = (double)(m1 * ngk + m2);  // position in the reference's (m1, m2) loop
-      r.pad[2] = 0.0;
+      r.pad[2] = (r.fact * r.coef) * r.p_inv;  // w: the pair's factor of the quartet prefactor
       out[o++] = r;
     }
 }
@@ -163,11 +163,9 @@ cudaError_t eri_init_constants() { return cudaSuccess; }  // tables are compile-
 
 // ket pairs per shared-memory tile and the dynamic shared memory it needs
 void eri_tile(int LK, bool t2, int max_cnt, int* ktile, size_t* smem) {
-  const int no = t2 ? 4 : 1;
   // per ket pair: the record and its polynomials (ket degree bound LK) in FP64, and their FP32
   // copies
-  const size_t per = sizeof(PrimPair) + sizeof(double) * 3 * no * (LK + 1) + 6 * sizeof(float) +
-                     sizeof(float) * 3 * no * (LK + 1);
+  const size_t per = eri_ket_bytes(LK, t2);
   // Small ket tiles: with ~53 KB of static tables and scans, 60 KB tiles let two CTAs share an
   // SM (8 warps) and leave unified L1 to the local arrays of the classes with r^2-type fits.  On
   // the 26-function H2O basis 168 KB (one CTA per SM) -> 60 KB tiles took the analytic stage from
@@ -298,7 +296,7 @@ __global__ void __launch_bounds__(512) prim_pair_sort(const PrimPair* __restrict
   for (int t = threadIdx.x; t < m; t += blockDim.x) dst[t] = src[s_idx[t]];
 }
 
-// FP32 copies of the (sorted) primitive pairs, fc = K_AB * coefficient product
+// FP32 copies of the (sorted) primitive pairs, fc = w = K_AB c p_inv
 __global__ void prim_pair_to_f32(int64_t npp, const PrimPair* __restrict__ in, PrimPairF* __restrict__ out) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= npp) return;
@@ -306,7 +304,7 @@ __global__ void prim_pair_to_f32(int64_t npp, const PrimPair* __restrict__ in, P
   PrimPairF f;
   f.p = (float)a.p;
   f.p_inv = (float)a.p_inv;
-  f.fc = (float)(a.fact * a.coef);
+  f.fc = (float)a.pad[2];
 #pragma unroll
   for (int ax = 0; ax < 3; ax++) {
     f.P[ax] = (float)a.P[ax];

@@ -308,26 +308,18 @@ SS_DFI void pair_polys(const QuartetShape& S, int side, const Rec& P, Real* out)
     }
 }
 
-// The fields of a primitive pair that one primitive quartet reads, in the arithmetic type of the
-// evaluation (FP64, or FP32 for the quartets below the FP32 bound).
-template <typename Real>
-struct PairView {
-  Real p, p_inv, P[3], fact;
-};
-
 SS_DFI PairView<double> view64(const PrimPair& A) {
-  return PairView<double>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fact};
+  return PairView<double>{A.p, A.p_inv, 0.5 * A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.pad[2]};
 }
 
-// FP32 view: fact carries K_AB times the coefficient product, so the FP32 quartet value comes
-// out already multiplied by the coefficients
 SS_DFI PairView<float> view32(const PrimPairF& A) {
-  return PairView<float>{A.p, A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fc};
+  return PairView<float>{A.p, A.p_inv, 0.5f * A.p_inv, {A.P[0], A.P[1], A.P[2]}, A.fc};
 }
 
 // One primitive quartet (src/general_primitive_integral.F90, summed over the cartesian
-// components of the r^2-type fits): returns pref * sum_n d1[n] F_n; the caller multiplies by
-// the coefficient product P.coef * Q.coef.  Pn, Qn: pair_polys of the bra and ket pairs.
+// components of the r^2-type fits), times the coefficient product of src/gauss_ijkl.F90:137 and
+// divided by 2 pi^{5/2}: returns w_P w_Q / sqrt(p+q) * sum_n d1[n] F_n.  Pn, Qn: pair_polys of
+// the bra and ket pairs.
 // TC: the number of r^2-type fits among the four functions (0..4; with any, the subset recursion
 // over the axes below).  L bounds the per-axis degree of the bra pair, LK that of the ket pair
 // (Pn: [ax][o][L+1], Qn: [ax][o][LK+1]); the total degree is at most 3 (L + LK).
@@ -339,20 +331,22 @@ SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const R
   constexpr int LT = L + LK;                       // per-axis degree bound of the quartet
   constexpr int NF = (3 * LT < 16) ? 3 * LT : 16;
   const Real p = P.p, qq = Q.p;
-  // src/general_primitive_integral.F90:54-60, 142-146
-  const Real pq = P.p_inv * Real(0.5) * Q.p_inv;
+  // src/general_primitive_integral.F90:54-60, 142-146, with q/(p+q) and p/(p+q) formed once
+  // (the same quantities, reassociated: they give p10_2, p01_2, rho and each axis's C00, D00)
+  const Real pq = P.hp * Q.p_inv;    // p_inv q_inv / 2
   const Real rs_pq = rsqrt(p + qq);  // 1/sqrt(p+q): gives 1/(p+q) and the prefactor's root
   const Real pq_inv = Real(0.5) * (rs_pq * rs_pq);
   RecCoefT<Real> R;
   R.p10_1 = qq * pq;
   R.p01_1 = p * pq;
   const Real pq_inv_2 = pq_inv + pq_inv;
-  R.p10_2 = pq_inv_2 * R.p10_1 * qq;
-  R.p01_2 = pq_inv_2 * R.p01_1 * p;
+  const Real fq = qq * pq_inv_2, fp = p * pq_inv_2;  // q/(p+q), p/(p+q)
+  R.p10_2 = R.p10_1 * fq;
+  R.p01_2 = R.p01_1 * fp;
   R.pq_inv = pq_inv;
-  const Real rho = p * qq * pq_inv_2;
-  const Real dx = P.P[0] - Q.P[0], dy = P.P[1] - Q.P[1], dz = P.P[2] - Q.P[2];
-  const Real T = (dx * dx + dy * dy + dz * dz) * rho;
+  const Real rho = p * fq;
+  const Real dP[3] = {P.P[0] - Q.P[0], P.P[1] - Q.P[1], P.P[2] - Q.P[2]};
+  const Real T = (dP[0] * dP[0] + dP[1] * dP[1] + dP[2] * dP[2]) * rho;
   Real F[NF + 1];
   if constexpr (sizeof(Real) == 8)
     boys_tab<NF>(T, S.nf, F, s_boys);
@@ -374,35 +368,48 @@ SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const R
         continue;
       }
       Real I[L + 1][LK + 1][LT + 1];
-      const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;  // src/give_polynom_mult_center_x.F90:58
-      const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;   // :62
+      const Real Cc = -fq * dP[ax];  // src/give_polynom_mult_center_x.F90:58
+      const Real Dd = fp * dP[ax];   // :62
       if (S.onec) rys_table_1c<L, LK>(R, S.amax[ax], S.cmax[ax], I);
       else rys_table<L, LK>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       axis_poly<L, LK>(Pn + ax * (L + 1), S.amax[ax], Qn + ax * (LK + 1), S.cmax[ax], I, ax == 0, A[ax]);
     }
-    // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173)
+    // d1 = (Ix Iy) Iz, then sum_n d1[n] F_n (src/general_primitive_integral.F90:148-173).  An
+    // axis of degree 0 has the polynomial 1, and a product with it is a copy (fma(1, x, 0) = x
+    // exactly), taken without the multiply-adds: quartet-uniform branches
     Real dp[2 * LT + 1];
+    if (deg[0] == 0 || deg[1] == 0) {
+      const bool x1 = deg[0] == 0;
 #pragma unroll
-    for (int t = 0; t <= 2 * LT; t++) dp[t] = Real(0);
+      for (int t = 0; t <= 2 * LT; t++) dp[t] = t <= LT ? (x1 ? A[1][t % (LT + 1)] : A[0][t % (LT + 1)]) : Real(0);
+    } else {
 #pragma unroll
-    for (int a = 0; a <= LT; a++) {
-      if (a > deg[0]) break;
+      for (int t = 0; t <= 2 * LT; t++) dp[t] = Real(0);
 #pragma unroll
-      for (int c = 0; c <= LT; c++) {
-        if (c > deg[1]) break;
-        dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
+      for (int a = 0; a <= LT; a++) {
+        if (a > deg[0]) break;
+#pragma unroll
+        for (int c = 0; c <= LT; c++) {
+          if (c > deg[1]) break;
+          dp[a + c] = fma(A[1][c], A[0][a], dp[a + c]);
+        }
       }
     }
     Real d1[NF + 1];
+    if (deg[2] == 0) {
 #pragma unroll
-    for (int t = 0; t <= NF; t++) d1[t] = Real(0);
+      for (int t = 0; t <= NF; t++) d1[t] = t <= 2 * LT ? dp[t % (2 * LT + 1)] : Real(0);
+    } else {
 #pragma unroll
-    for (int a = 0; a <= 2 * LT; a++) {
-      if (a > deg[0] + deg[1] || a > NF) break;
+      for (int t = 0; t <= NF; t++) d1[t] = Real(0);
 #pragma unroll
-      for (int c = 0; c <= LT; c++) {
-        if (c > deg[2] || a + c > NF) break;
-        d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
+      for (int a = 0; a <= 2 * LT; a++) {
+        if (a > deg[0] + deg[1] || a > NF) break;
+#pragma unroll
+        for (int c = 0; c <= LT; c++) {
+          if (c > deg[2] || a + c > NF) break;
+          d1[a + c] = fma(A[2][c], dp[a], d1[a + c]);
+        }
       }
     }
     accu = d1[0] * F[0];
@@ -422,8 +429,8 @@ SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const R
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       Real I[L + 1][LK + 1][LT + 1];
-      const Real Cc = -qq * (P.P[ax] - Q.P[ax]) * pq_inv_2;
-      const Real Dd = -p * (Q.P[ax] - P.P[ax]) * pq_inv_2;
+      const Real Cc = -fq * dP[ax];
+      const Real Dd = fp * dP[ax];
       if (S.onec) rys_table_1c<L, LK>(R, S.amax[ax], S.cmax[ax], I);
       else rys_table<L, LK>(R, Cc, Dd, S.amax[ax], S.cmax[ax], I);
       if (ax == 1) {
@@ -482,9 +489,8 @@ SS_DFI Real prim_quartet(const QuartetShape& S, const PairView<Real>& P, const R
       }
     }
   }
-  // src/general_primitive_integral.F90:192
-  const Real pref = P.fact * Q.fact * (Real)PI_5_2 * P.p_inv * Q.p_inv * rs_pq;
-  return pref * accu;
+  // src/general_primitive_integral.F90:192 without its constant 2 pi^{5/2}
+  return (P.w * Q.w * rs_pq) * accu;
 }
 
 #ifdef __CUDACC__
@@ -536,11 +542,21 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
   __shared__ int s_scan32[SS_MAX_NG * SS_MAX_NG + 1];  // FP32 item offsets
   __shared__ double s_boys[BOYS_SMEM_DOUBLES];
   __shared__ float s_boys32[BOYS32_K * BOYS32_N];
+  const int64_t w = blockIdx.x / split;
+  const int part = blockIdx.x % split;
+  {  // the launch's dynamic shared memory must hold ktile staged ket pairs: checked, not assumed
+    uint32_t dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const size_t need =
+        (size_t)ktile * (sizeof(PrimPair) + (size_t)QW * (sizeof(double) + sizeof(float)) + sizeof(PairView<float>));
+    if (need > dyn) {  // block-uniform: no thread reaches a barrier
+      if (threadIdx.x == 0) partial[w * split + part] = __longlong_as_double(0x7FF8000000000000LL);
+      return;
+    }
+  }
   boys_tables_to_smem(s_boys);  // ordered before first use by the tile loop's barriers
   for (int t = threadIdx.x; t < BOYS32_K * BOYS32_N; t += blockDim.x) s_boys32[t] = boys32_tab[t];
 
-  const int64_t w = blockIdx.x / split;
-  const int part = blockIdx.x % split;
   const int64_t wq = work[w];
   const int64_t q = wq & ((int64_t(1) << 62) - 1);
   const bool swp = (wq >> 62) & 1;  // evaluate (jl|ik)
@@ -663,11 +679,10 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
         const double v =
             prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(Q), s_q + (size_t)ik * QW, s_boys);
         if (self_out) {
-          self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax((P.coef * Q.coef) * v, 0.0));
+          self_out[16 * (pair_off[pb] + ib)] = sqrt(fmax(PI_5_2 * v, 0.0));
           continue;
         }
-        // the coefficient product of src/gauss_ijkl.F90:137
-        acc = fma(P.coef * Q.coef, v, acc);
+        acc += v;
       }
     }
     {  // FP32 tier: the ket range [c64, c) of each bra pair
@@ -705,7 +720,7 @@ __global__ void __launch_bounds__(128, 1) eri_kernel(
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) partial[w * split + part] = ((s_red[0] + s_red[1]) + s_red[2]) + s_red[3];
+  if (threadIdx.x == 0) partial[w * split + part] = PI_5_2 * (((s_red[0] + s_red[1]) + s_red[2]) + s_red[3]);
 }
 
 #endif  // __CUDACC__

@@ -66,15 +66,34 @@ struct __align__(16) PrimPair {
   double coef;           // c(m1,i) * c(m2,k)
   double PA[3];          // P - A  (pows_a(1) of src/give_explicit_poly_and_gaussian.F90:125)
   double PB[3];          // P - B
-  double pad[3];         // [0] Schwarz factor sqrt(coef^2 (P|P)), [1] index m1*ng(k)+m2, [2] unused
+  double pad[3];         // [0] Schwarz factor sqrt(coef^2 (P|P)), [1] index m1*ng(k)+m2,
+                         // [2] w = fact * coef * p_inv
 };
 static_assert(sizeof(PrimPair) == 16 * sizeof(double), "PrimPair is 16 doubles (the kernels stride by 16)");
 
-// FP32 copy of a primitive pair for the primitive quartets evaluated in FP32: fc = K_AB * coef.
+// FP32 copy of a primitive pair for the primitive quartets evaluated in FP32: fc = w = K_AB c p_inv.
 struct __align__(16) PrimPairF {
   float p, p_inv, P[3], fc, PA[3], PB[3], pad[2];
 };
 static_assert(sizeof(PrimPairF) == 16 * sizeof(float), "PrimPairF is 16 floats");
+
+// The fields of a primitive pair that one primitive quartet reads, in the arithmetic type of the
+// evaluation (FP64, or FP32 for the quartets below the FP32 bound); the ERI kernel keeps the FP32
+// views of a ket tile in shared memory.  w = K_AB c p_inv, the pair's factor of the primitive
+// quartet's prefactor (the constant 2 pi^{5/2} of src/general_primitive_integral.F90:192 is
+// applied once to the contracted sum); hp = p_inv / 2 (exact).
+template <typename Real>
+struct PairView {
+  Real p, p_inv, hp, P[3], w;
+};
+
+// Shared memory of the ERI kernel per staged ket pair: the FP64 record and its recentred
+// polynomials (3 axes x options x (LK + 1)), the FP32 view and the FP32 polynomials -- the
+// kernel's carve-up of its dynamic shared memory, in the same order.
+inline size_t eri_ket_bytes(int LK, bool t2) {
+  const size_t qw = 3 * (t2 ? 4 : 1) * (size_t)(LK + 1);
+  return sizeof(PrimPair) + sizeof(double) * qw + sizeof(PairView<float>) + sizeof(float) * qw;
+}
 
 // Device view of the fitted basis (Fortran layouts, 0-based).
 struct BasisDev {

@@ -8,8 +8,8 @@
 * EXEC_FLOPS: executed flops of all eri_kernel launches of one job (Schwarz factors, Schwarz
   diagonal and screened quartets), from ncu instruction counters on the full workload
   (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd,ffma}_pred_on.sum, one pass each; DFMA
-  and FFMA counted as 2 flops), and EXEC_DRAM_BYTES their DRAM traffic.  Command and per-class
-  table: profiles/eri_kernel_h2o26.md.
+  and FFMA counted as 2 flops), and EXEC_DRAM_BYTES their DRAM traffic (the per-class table and
+  the command are kept with the profiles).
 * EXEC_FLOPS_PER_PRIM: the earlier all-FP64 kernel's executed FP64 flops per primitive quartet
   (241.5, unscreened), kept as the model for workloads without a measurement.
 """
@@ -23,13 +23,19 @@ EXEC_FLOPS_PER_PRIM = 241.5
 # workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job, at
 # the default tiers (primitive screen 1e-18, FP32 tier below 1e-11 of the Schwarz bound)
 EXEC_FLOPS = {
-    "h2o_26_ng20": (5.878e11, 4.787e11),
+    "h2o_26_ng20": (5.554e11, 4.698e11),
 }
 # workload -> DRAM bytes (read + write) of all eri_kernel launches of one job (ncu
 # dram__bytes_read.sum + dram__bytes_write.sum, one pass each; mostly the local-memory spill
 # traffic of the L = 4 classes with several r^2-type fits)
+# workload -> DRAM bytes per walker pair of the shared-walker MC kernels (sampler, orbital values,
+# operands, tcgen05 GEMM, accumulation): ncu --set full of one 262,144-sample sub-chunk (reads
+# 2.0146e9 B + writes 1.5291e9 B) / 262,144
+MC_DRAM_BYTES_PER_SAMPLE = {
+    "h2o_26_ng20": 3.5437e9 / 262144,
+}
 EXEC_DRAM_BYTES = {
-    "h2o_26_ng20": 1.157e10,  # 1.1570e10 (with the LK = 0, 1 light-ket instances of L <= 3)
+    "h2o_26_ng20": 1.2104e10,
 }
 
 

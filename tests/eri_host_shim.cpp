@@ -69,6 +69,7 @@ std::vector<PrimPair> build_pairs(const BasisDev& B, int i, int k, bool fold_ena
       r.coef = B.c_gauss[m1 + (int64_t)B.ld * (i + (int64_t)B.n * ti)] *
                B.c_gauss[m2 + (int64_t)B.ld * (k + (int64_t)B.n * tk)];
       if (fold && m1 != m2) r.coef = 2.0 * r.coef;
+      r.pad[2] = (r.fact * r.coef) * r.p_inv;
       out.push_back(r);
     }
   return out;
@@ -99,11 +100,10 @@ double quartet_value(const BasisDev& B, int fi, int fk, int fj, int fl, bool fol
   for (const PrimPair& P : bra) {
     pair_polys<L, T2, double>(S, 0, P, Pn);
     for (size_t t = 0; t < ket.size(); t++) {
-      const double v = prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
-      acc = std::fma(P.coef * ket[t].coef, v, acc);
+      acc += prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
     }
   }
-  return acc;
+  return PI_5_2 * acc;
 }
 
 // the instance launch_eri_class (csrc/eri.cu) runs for (L, LK, tc): SS_HOST_DISPATCH(F, args)
@@ -176,7 +176,7 @@ std::vector<double> self_factors(const BasisDev& B, int i, int k, const std::vec
     pair_polys<L, T2, double>(S, 0, pairs[t], Pn);
     pair_polys<LK, T2, double>(S, 1, pairs[t], Qn);
     const double v = prim_quartet<L, TC, double, LK>(S, view64(pairs[t]), Pn, view64(pairs[t]), Qn, tab);
-    out[t] = std::sqrt(std::fmax((pairs[t].coef * pairs[t].coef) * v, 0.0));
+    out[t] = std::sqrt(std::fmax(PI_5_2 * v, 0.0));
   }
   return out;
 }
@@ -193,7 +193,7 @@ PrimPairF to_f32(const PrimPair& a) {  // prim_pair_to_f32 (csrc/eri.cu)
   PrimPairF f{};
   f.p = (float)a.p;
   f.p_inv = (float)a.p_inv;
-  f.fc = (float)(a.fact * a.coef);
+  f.fc = (float)a.pad[2];
   for (int ax = 0; ax < 3; ax++) {
     f.P[ax] = (float)a.P[ax];
     f.PA[ax] = (float)a.PA[ax];
@@ -243,21 +243,22 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, d
     pair_polys<L, T2, double>(S, 0, P, Pn);
     pair_polys<L, T2, float>(S, 0, P32, Pf);
     for (size_t t = 0; t < ket.size(); t++) {
-      const double v64 =
-          (P.coef * ket[t].coef) * prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
-      const float v32 =
+      // both tiers return the term divided by 2 pi^{5/2} (the kernel applies it to the sum)
+      const double v64 = PI_5_2 * prim_quartet<L, TC, double, LK>(S, view64(P), Pn, view64(ket[t]), &q[t * QW], tab);
+      const float t32 =
           prim_quartet<L, TC, float, LK>(S, view32(P32), Pf, view32(to_f32(ket[t])), &qf[t * QW], boys32_tab);
+      const double v32 = PI_5_2 * (double)t32;
       const double bound = Sb[b] * Sk[t];
       if (!(bound > 0.0)) continue;
-      const double r = std::fabs((double)v32 - v64) / bound;
+      const double r = std::fabs(v32 - v64) / bound;
       e->all = std::max(e->all, r);
       e->n_all++;
       if (bound < eps32 * sch) {
         e->tier = std::max(e->tier, r);
         e->n_tier++;
-        s_signed += (double)v32 - v64;
-        s_abs += std::fabs((double)v32 - v64);
-        tier_terms.push_back(v32);
+        s_signed += v32 - v64;
+        s_abs += std::fabs(v32 - v64);
+        tier_terms.push_back(t32);
       }
     }
   }
@@ -274,7 +275,7 @@ int fp32_errors(const BasisDev& B, int fi, int fk, int fj, int fl, double sch, d
       }
       dev += (double)acc32;
     }
-    e->q_acc = std::max(e->q_acc, std::fabs(dev - exact) / sch);
+    e->q_acc = std::max(e->q_acc, PI_5_2 * std::fabs(dev - exact) / sch);
   }
   return 0;
 }
