@@ -44,8 +44,9 @@ class JobAdmission {
     cv_.notify_all();
   }
 
-  // blocks until the job may start; the caller must release(bytes) when it ends
-  void admit(int64_t ticket, size_t bytes) {
+  // blocks until the job may start; the caller must release(bytes) when it ends.  Returns the
+  // job's rank among the admitted jobs (0, 1, ...), taken under the admission's lock.
+  int64_t admit(int64_t ticket, size_t bytes) {
     std::unique_lock<std::mutex> lk(mu_);
     cv_.wait(lk, [&] {
       if (head_ != ticket) return false;
@@ -60,6 +61,7 @@ class JobAdmission {
     head_++;
     advance_head();
     cv_.notify_all();
+    return admitted_++;
   }
 
   void release(size_t bytes) {
@@ -92,7 +94,7 @@ class JobAdmission {
   std::condition_variable cv_;
   size_t budget_ = 0, used_ = 0, peak_used_ = 0;
   int max_running_ = 0, running_ = 0, peak_running_ = 0;
-  int64_t next_ = 0, head_ = 0;
+  int64_t next_ = 0, head_ = 0, admitted_ = 0;
   std::set<int64_t> skipped_;
 };
 

@@ -21,7 +21,7 @@ int ss_host_admission_run(int njobs, const long long* bytes, const int* abandon,
   ss::JobAdmission adm;
   adm.set_limits((size_t)budget, max_running);
   std::mutex mu;
-  int running = 0, next_start = 0;
+  int running = 0;
   long long used = 0;
   *peak_running = 0;
   *peak_bytes = 0;
@@ -36,10 +36,12 @@ int ss_host_admission_run(int njobs, const long long* bytes, const int* abandon,
       continue;
     }
     th.emplace_back([&, j, ticket]() {
-      adm.admit(ticket, (size_t)bytes[j]);
+      // the rank is taken inside the admission's critical section: two jobs admitted back to
+      // back may reach the lock below in either order
+      const int64_t rank = adm.admit(ticket, (size_t)bytes[j]);
       {
         std::lock_guard<std::mutex> lk(mu);
-        start_order[j] = next_start++;
+        start_order[j] = (int)rank;
         running++;
         used += bytes[j];
         if (running > *peak_running) *peak_running = running;
