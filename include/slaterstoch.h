@@ -209,7 +209,10 @@ int ss_set_exact_monocenter(ss_ctx* ctx, int enable);
 double ss_mc_max_sigma(const ss_ctx* ctx);
 int ss_mc_blocks_done(const ss_ctx* ctx);
 
-/* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+/* The context's CUDA stream (cudaStream_t, created with the device's greatest stream priority).
+ * Every call's work is ordered on it: the internal side streams (the analytic ERI classes, and in
+ * ss_two_e_job the whole analytic stage running beside the MC, at the lowest priority) fork from
+ * it and join back into it before the call returns. */
 void* ss_stream(ss_ctx* ctx);
 
 /* The shared estimator's tensor-core contraction on caller data (no reference counterpart;
