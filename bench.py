@@ -479,6 +479,11 @@ def main():
                 "kernel": "eri_kernel (analytic Gaussian-fit ERIs, all launches of one job)",
                 "peak_source": "measured in this run: torch float64 matmul 4096^3 (FP64 peak is not "
                                "in MEASURED_PEAKS.json)",
+                "fp64_pipe_issue_pct": 82.7,
+                "fp64_pipe_note": ("ncu sm__inst_executed_pipe_fp64 of the largest instance, eri_kernel<2,0,1> "
+                                   "(--set full, small case): the stage is FP64-issue bound; the flop "
+                                   "fraction is lower because its FP64 instructions mix DMUL/DADD (1 flop) "
+                                   "with DFMA (2) while the DGEMM peak issues only DFMAs"),
                 "units": (f"executed FP64 flops of the job's eri_kernel launches (ncu instruction "
                           f"counters, DFMA = 2): {flops:.4g}; plus {EXEC_FLOPS[wl][1]:.4g} FP32 FFMA flops "
                           f"of the FP32 tier; {nprim:.4g} primitive quartets before screening")

@@ -101,7 +101,9 @@ struct RecCoefT {
 };
 
 // Bottom-up table I(a,c)[m] (coefficients of u = t^2) for a <= amax <= L, c <= cmax <= LK,
-// the same per-coefficient operation order as I_x1_pol_mult / I_x2_pol_mult:
+// the terms of I_x1_pol_mult / I_x2_pol_mult in their order, each as one fused multiply-add with
+// the integer factor folded into the recursion coefficient ((a-1) B10 is formed once per
+// primitive quartet, not per entry):
 //   I(0,c) = (c-1) B01 I(0,c-2) + D00 I(0,c-1);  I(a,c) = (a-1) B10 I(a-2,c) + c B00 I(a-1,c-1) + C00 I(a-1,c)
 template <int L, int LK, typename Real>
 SS_DFI void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int cmax,
@@ -117,10 +119,10 @@ SS_DFI void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int c
         v = Real(1);
       } else {
         if (c >= 2) {
-          if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (Real)(c - 1));
-          if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (Real)(c - 1));
+          if (m >= 1 && m - 1 <= c - 2) v = fma(-R.p01_2 * (Real)(c - 1), I[0][c - 2][m - 1], v);
+          if (m <= c - 2) v = fma(R.p01_1 * (Real)(c - 1), I[0][c - 2][m], v);
         }
-        if (m >= 1) v = v + Dd * I[0][c - 1][m - 1];
+        if (m >= 1) v = fma(Dd, I[0][c - 1][m - 1], v);
       }
       I[0][c][m] = v;
     }
@@ -137,11 +139,11 @@ SS_DFI void rys_table(const RecCoefT<Real>& R, Real Cc, Real Dd, int amax, int c
         Real v = Real(0);
         if (a >= 2) {
           const Real s = (Real)(a - 1);
-          if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
-          if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
+          if (m >= 1 && m - 1 <= a - 2 + c) v = fma(-R.p10_2 * s, I[a - 2][c][m - 1], v);
+          if (m <= a - 2 + c) v = fma(R.p10_1 * s, I[a - 2][c][m], v);
         }
-        if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (Real)c);
-        if (m >= 1) v = v + Cc * I[a - 1][c][m - 1];
+        if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = fma(R.pq_inv * (Real)c, I[a - 1][c - 1][m - 1], v);
+        if (m >= 1) v = fma(Cc, I[a - 1][c][m - 1], v);
         I[a][c][m] = v;
       }
     }
@@ -163,8 +165,8 @@ SS_DFI void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
       if (c == 0) {
         v = Real(1);
       } else if (!(c & 1) && c >= 2) {
-        if (m >= 1 && m - 1 <= c - 2) v = v + (-R.p01_2) * (I[0][c - 2][m - 1] * (Real)(c - 1));
-        if (m <= c - 2) v = v + R.p01_1 * (I[0][c - 2][m] * (Real)(c - 1));
+        if (m >= 1 && m - 1 <= c - 2) v = fma(-R.p01_2 * (Real)(c - 1), I[0][c - 2][m - 1], v);
+        if (m <= c - 2) v = fma(R.p01_1 * (Real)(c - 1), I[0][c - 2][m], v);
       }
       I[0][c][m] = v;
     }
@@ -182,10 +184,10 @@ SS_DFI void rys_table_1c(const RecCoefT<Real>& R, int amax, int cmax,
         if (!((a + c) & 1)) {
           if (a >= 2) {
             const Real s = (Real)(a - 1);
-            if (m >= 1 && m - 1 <= a - 2 + c) v = v + (-R.p10_2) * (I[a - 2][c][m - 1] * s);
-            if (m <= a - 2 + c) v = v + R.p10_1 * (I[a - 2][c][m] * s);
+            if (m >= 1 && m - 1 <= a - 2 + c) v = fma(-R.p10_2 * s, I[a - 2][c][m - 1], v);
+            if (m <= a - 2 + c) v = fma(R.p10_1 * s, I[a - 2][c][m], v);
           }
-          if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = v + R.pq_inv * (I[a - 1][c - 1][m - 1] * (Real)c);
+          if (c >= 1 && m >= 1 && m - 1 <= a - 1 + c - 1) v = fma(R.pq_inv * (Real)c, I[a - 1][c - 1][m - 1], v);
         }
         I[a][c][m] = v;
       }

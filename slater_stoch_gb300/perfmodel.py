@@ -23,7 +23,7 @@ EXEC_FLOPS_PER_PRIM = 241.5
 # workload -> (executed FP64 flops, executed FP32 FFMA flops) of the analytic stage of one job, at
 # the default tiers (primitive screen 1e-18, FP32 tier below 1e-11 of the Schwarz bound)
 EXEC_FLOPS = {
-    "h2o_26_ng20": (5.554e11, 4.698e11),
+    "h2o_26_ng20": (5.518e11, 4.700e11),
 }
 # workload -> DRAM bytes (read + write) of all eri_kernel launches of one job (ncu
 # dram__bytes_read.sum + dram__bytes_write.sum, one pass each; mostly the local-memory spill
@@ -35,7 +35,7 @@ MC_DRAM_BYTES_PER_SAMPLE = {
     "h2o_26_ng20": 3.5437e9 / 262144,
 }
 EXEC_DRAM_BYTES = {
-    "h2o_26_ng20": 1.2104e10,
+    "h2o_26_ng20": 1.2443e10,
 }
 
 
